@@ -1,0 +1,347 @@
+"""2dtissue_gb300 — GB300-native per-step active-particle update of 2DTissue.
+
+Thin Python harness over the C-ABI in include/tds.h (ctypes). The package name starts with a
+digit, so import it with ``importlib.import_module("2dtissue_gb300")``.
+
+Objects:
+  Mesh        closed surface + unit-square UV chart (icosphere ellipsoid, bumpy sphere, OFF file)
+  Simulation  one system (R = 1) or a ragged ensemble of replicas on one mesh
+  Tissue      the reference's _2DTissue interface: start(), update(), is_finished(),
+              get_order_parameter() (src/simulation/2DTissue.h:37-60)
+
+The CUDA library is required: every simulation call fails loudly (RuntimeError) when the
+extension is missing or there is no GPU. There is no CPU fallback.
+"""
+import ctypes as C
+import os
+from dataclasses import dataclass, asdict
+
+import numpy as np
+
+from . import build as _build
+
+TDS_OK = 0
+ERRORS = {1: "invalid argument", 2: "CUDA error / no CUDA device", 3: "mesh error", 4: "device status set",
+          5: "out of device memory", 6: "size limit"}
+STATUS_BITS = {1: "non-finite", 2: "wrap limit", 4: "locate fallback", 8: "neighbour overflow",
+               16: "cell overflow", 32: "scan timeout"}
+
+_lib = None
+
+
+class TdsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("tds error %d (%s): %s" % (code, ERRORS.get(code, "?"), msg))
+        self.code = code
+
+
+class _Params(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("radius", "k_rep", "k_adh", "r_max", "v0", "mu", "tau", "align",
+                                          "eta", "dt")] + [("force_mode", C.c_int), ("reserved", C.c_int)]
+
+
+class _StateView(C.Structure):
+    _fields_ = [("uv", C.c_void_p), ("theta", C.c_void_p), ("face", C.c_void_p), ("r3d", C.c_void_p),
+                ("vel_uv", C.c_void_p), ("nbr_count", C.c_void_p)]
+
+
+def library_path():
+    return _build.LIB
+
+
+def lib(build_if_missing=True):
+    """Loads (building if needed) the in-tree CUDA library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError("lib2dtissue_gb300.so is not built (run __graft_entry__.build())")
+        _build.build()
+    L = C.CDLL(path)
+    P, I, D, VP = C.POINTER, C.c_int, C.c_double, C.c_void_p
+    L.tds_mesh_ellipsoid.argtypes = [I, D, D, D, P(VP)]
+    L.tds_mesh_bumpy_sphere.argtypes = [I, D, D, P(VP)]
+    L.tds_mesh_from_arrays.argtypes = [VP, I, VP, I, P(VP)]
+    L.tds_mesh_load_off.argtypes = [C.c_char_p, P(VP)]
+    L.tds_mesh_save_off.argtypes = [VP, C.c_char_p]
+    L.tds_mesh_info.argtypes = [VP, P(I), P(I), P(I), P(D)]
+    L.tds_mesh_arrays.argtypes = [VP, VP, VP, VP, VP, VP]
+    L.tds_mesh_destroy.argtypes = [VP]
+    L.tds_mesh_last_error.restype = C.c_char_p
+    L.tds_create.argtypes = [VP, P(_Params), I, C.c_uint64, I, P(VP)]
+    L.tds_ensemble_create.argtypes = [VP, I, VP, VP, C.c_uint64, I, P(VP)]
+    L.tds_start.argtypes = [VP]
+    L.tds_step.argtypes = [VP, I, VP]
+    L.tds_update.argtypes = [VP, P(_StateView)]
+    L.tds_set_state.argtypes = [VP, P(_StateView)]
+    L.tds_get_state.argtypes = [VP, P(_StateView)]
+    L.tds_get_order_parameter.argtypes = [VP, VP, VP, I, P(I)]
+    L.tds_get_step.argtypes = [VP, P(C.c_int64)]
+    L.tds_get_status.argtypes = [VP, P(I)]
+    L.tds_clear_status.argtypes = [VP]
+    L.tds_num_particles.argtypes = [VP, P(I), P(I)]
+    L.tds_stream.argtypes = [VP, P(VP)]
+    L.tds_step_async.argtypes = [VP, I]
+    L.tds_kernel_timing.argtypes = [VP, I]
+    L.tds_kernel_times.argtypes = [VP, VP, VP]
+    L.tds_kernels_per_step.argtypes = [VP, P(I)]
+    L.tds_last_error.argtypes = [VP]
+    L.tds_last_error.restype = C.c_char_p
+    L.tds_destroy.argtypes = [VP]
+    L.tds_debug_seam_wrap.argtypes = [I, VP, VP, VP, VP, VP, I]
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+@dataclass
+class Params:
+    """Model parameters; defaults are the config-1 values (radius 0.05, r_max = 2.4 R)."""
+    radius: float = 0.05
+    k_rep: float = 10.0
+    k_adh: float = 0.75
+    r_max: float = 0.12
+    v0: float = 1.0
+    mu: float = 1.0
+    tau: float = 1.0
+    align: float = 0.5
+    eta: float = 0.5
+    dt: float = 0.02
+    force_mode: int = 0
+
+    def to_c(self):
+        p = _Params()
+        for k, v in asdict(self).items():
+            setattr(p, k, v)
+        return p
+
+    def oracle_dict(self):
+        return dict(R=self.radius, k=self.k_rep, k_adh=self.k_adh, r_max=self.r_max, v0=self.v0, mu=self.mu,
+                    tau=self.tau, align=self.align, eta=self.eta, dt=self.dt)
+
+
+class Mesh:
+    """Closed triangulated surface with its unit-square UV chart."""
+
+    def __init__(self, handle):
+        self.h = C.c_void_p(handle)
+        V, F, Vuv, A = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        lib().tds_mesh_info(self.h, C.byref(V), C.byref(F), C.byref(Vuv), C.byref(A))
+        self.V, self.F, self.Vuv, self.area = V.value, F.value, Vuv.value, A.value
+
+    @staticmethod
+    def _make(fn, *args):
+        h = C.c_void_p()
+        rc = fn(*args, C.byref(h))
+        if rc != TDS_OK:
+            raise TdsError(rc, lib().tds_mesh_last_error().decode())
+        return Mesh(h.value)
+
+    @classmethod
+    def ellipsoid(cls, level, axes=(1.0, 1.0, 1.0)):
+        return cls._make(lib().tds_mesh_ellipsoid, int(level), *map(float, axes))
+
+    @classmethod
+    def bumpy_sphere(cls, level, amp=0.2, scale=5.0):
+        return cls._make(lib().tds_mesh_bumpy_sphere, int(level), float(amp), float(scale))
+
+    @classmethod
+    def from_arrays(cls, v3, f3):
+        v3 = np.ascontiguousarray(v3, np.float64)
+        f3 = np.ascontiguousarray(f3, np.int32)
+        return cls._make(lib().tds_mesh_from_arrays, v3.ctypes.data, len(v3), f3.ctypes.data, len(f3))
+
+    @classmethod
+    def load_off(cls, path):
+        return cls._make(lib().tds_mesh_load_off, os.fsencode(path))
+
+    def save_off(self, path):
+        rc = lib().tds_mesh_save_off(self.h, os.fsencode(path))
+        if rc:
+            raise TdsError(rc, lib().tds_mesh_last_error().decode())
+
+    def arrays(self):
+        v3 = np.zeros((self.V, 3))
+        f3 = np.zeros((self.F, 3), np.int32)
+        uv = np.zeros((self.Vuv, 2))
+        fuv = np.zeros((self.F, 3), np.int32)
+        uv2v = np.zeros(self.Vuv, np.int32)
+        lib().tds_mesh_arrays(self.h, v3.ctypes.data, f3.ctypes.data, uv.ctypes.data, fuv.ctypes.data,
+                              uv2v.ctypes.data)
+        return dict(v3=v3, f3=f3, uv=uv, fuv=fuv, uv2v=uv2v)
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and _lib is not None:
+            _lib.tds_mesh_destroy(self.h)
+            self.h = None
+
+
+class Simulation:
+    """One system (n_particles int) or a ragged ensemble (n_particles list, params list)."""
+
+    def __init__(self, mesh, params, n_particles, seed=0, precision=32):
+        self.mesh = mesh
+        L = lib()
+        h = C.c_void_p()
+        if np.ndim(n_particles) == 0:
+            self.params = [params]
+            p = params.to_c()
+            rc = L.tds_create(mesh.h, C.byref(p), int(n_particles), C.c_uint64(seed), int(precision), C.byref(h))
+        else:
+            n = np.ascontiguousarray(n_particles, np.int32)
+            ps = list(params) if isinstance(params, (list, tuple)) else [params] * len(n)
+            self.params = ps
+            arr = (_Params * len(n))(*[q.to_c() for q in ps])
+            rc = L.tds_ensemble_create(mesh.h, len(n), n.ctypes.data, C.cast(arr, C.c_void_p), C.c_uint64(seed),
+                                       int(precision), C.byref(h))
+        if rc != TDS_OK:
+            raise TdsError(rc, "create failed (no CUDA device, bad parameters or size limit)")
+        self.h = h
+        nt, nr = C.c_int(), C.c_int()
+        L.tds_num_particles(self.h, C.byref(nt), C.byref(nr))
+        self.N, self.R = nt.value, nr.value
+        self.precision = precision
+        self.seed = seed
+
+    def _check(self, rc):
+        if rc != TDS_OK:
+            raise TdsError(rc, lib().tds_last_error(self.h).decode())
+
+    def start(self):
+        self._check(lib().tds_start(self.h))
+
+    def step(self, n=1, noise=None):
+        nz = None if noise is None else np.ascontiguousarray(noise, np.float64)
+        if nz is not None and nz.size != n * self.N:
+            raise ValueError("noise must have n_steps * N entries")
+        self._check(lib().tds_step(self.h, int(n), _ptr(nz)))
+
+    def step_async(self, n=1):
+        """Launches n steps without waiting (status checked by the next step() / status())."""
+        self._check(lib().tds_step_async(self.h, int(n)))
+
+    def kernel_timing(self, enable=True):
+        self._check(lib().tds_kernel_timing(self.h, int(bool(enable))))
+
+    def kernel_times(self):
+        """{name: (total_ms, launches)} for scan, scatter, step, finalize."""
+        ms = np.zeros(4)
+        n = np.zeros(4, np.int64)
+        self._check(lib().tds_kernel_times(self.h, ms.ctypes.data, n.ctypes.data))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(("scan", "scatter", "step", "finalize"))}
+
+    def set_state(self, uv, theta, face=None, r3d=None):
+        uv = np.ascontiguousarray(uv, np.float64)
+        th = np.ascontiguousarray(theta, np.float64)
+        fc = None if face is None else np.ascontiguousarray(face, np.int32)
+        r3 = None if r3d is None else np.ascontiguousarray(r3d, np.float64)
+        v = _StateView(_ptr(uv), _ptr(th), _ptr(fc), _ptr(r3), None, None)
+        self._check(lib().tds_set_state(self.h, C.byref(v)))
+
+    def get_state(self, out=None):
+        N = self.N
+        o = out if out is not None else dict(uv=np.zeros((N, 2)), theta=np.zeros(N), face=np.zeros(N, np.int32),
+                                            r3d=np.zeros((N, 3)), vel_uv=np.zeros((N, 2)),
+                                            nbr=np.zeros(N, np.int32))
+        v = _StateView(_ptr(o["uv"]), _ptr(o["theta"]), _ptr(o["face"]), _ptr(o["r3d"]), _ptr(o.get("vel_uv")),
+                       _ptr(o.get("nbr")))
+        self._check(lib().tds_get_state(self.h, C.byref(v)))
+        return o
+
+    def order_parameter(self):
+        n = C.c_int()
+        lib().tds_get_order_parameter(self.h, None, None, 0, C.byref(n))
+        phi = np.zeros(n.value * self.R)
+        psi = np.zeros(n.value * self.R)
+        self._check(lib().tds_get_order_parameter(self.h, phi.ctypes.data, psi.ctypes.data, len(phi), C.byref(n)))
+        return phi.reshape(n.value, self.R), psi.reshape(n.value, self.R)
+
+    @property
+    def step_count(self):
+        s = C.c_int64()
+        lib().tds_get_step(self.h, C.byref(s))
+        return s.value
+
+    def status(self):
+        s = C.c_int()
+        self._check(lib().tds_get_status(self.h, C.byref(s)))
+        return s.value
+
+    def clear_status(self):
+        self._check(lib().tds_clear_status(self.h))
+
+    def stream(self):
+        p = C.c_void_p()
+        self._check(lib().tds_stream(self.h, C.byref(p)))
+        return p.value
+
+    def kernels_per_step(self):
+        n = C.c_int()
+        self._check(lib().tds_kernels_per_step(self.h, C.byref(n)))
+        return n.value
+
+    def close(self):
+        if getattr(self, "h", None) is not None and _lib is not None:
+            _lib.tds_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Tissue:
+    """The reference facade (_2DTissue, src/simulation/2DTissue.h:37-60) over the GPU step.
+
+    Argument meaning follows the reference ctor: sigma is the particle radius, r_adh the
+    interaction cut-off, step_size the time step. The reference's CLI passes --step-time into
+    the v0 slot (main.cpp:76-84); here step_size is the time step, stated explicitly.
+    """
+
+    def __init__(self, save_data=False, particle_innenleben=False, free_boundary=False, mesh_path=None,
+                 particle_count=1000, step_count=1, v0=0.1, use_kafka=False, k=1.0, k_next=10.0, v0_next=0.1,
+                 sigma=0.4166666666666667, mu=1.0, r_adh=1.0, k_adh=0.75, step_size=0.001, map_cache_count=30,
+                 tau=1.0, align=0.5, eta=0.0, seed=0, precision=32, mesh=None):
+        self.mesh = mesh if mesh is not None else (Mesh.load_off(mesh_path) if mesh_path else Mesh.ellipsoid(4, (2, 1, 1)))
+        self.params = Params(radius=sigma, k_rep=k, k_adh=k_adh, r_max=r_adh, v0=v0, mu=mu, tau=tau, align=align,
+                             eta=eta, dt=step_size)
+        self.step_count = int(step_count)
+        self.current_step = 0
+        self.sim = Simulation(self.mesh, self.params, int(particle_count), seed=seed, precision=precision)
+
+    def start(self):
+        self.sim.start()
+
+    def update(self):
+        """One step; returns the System record: order parameter + per-particle arrays."""
+        self.sim.step(1)
+        self.current_step += 1
+        st = self.sim.get_state()
+        phi, _ = self.sim.order_parameter()
+        return dict(order_parameter=float(phi[-1, 0]), particles=st)
+
+    def is_finished(self):
+        return self.current_step >= self.step_count
+
+    def get_order_parameter(self):
+        phi, _ = self.sim.order_parameter()
+        return phi[:, 0]
+
+
+def debug_seam_wrap(uv_old, uv, theta=None, vel=None, precision=64):
+    """Device seam wrap on a batch of points (test hook)."""
+    uo = np.ascontiguousarray(uv_old, np.float64)
+    u = np.array(uv, np.float64, order="C")
+    n = len(u)
+    th = np.zeros(n) if theta is None else np.array(theta, np.float64)
+    v = np.zeros((n, 2)) if vel is None else np.array(vel, np.float64, order="C")
+    nw = np.zeros(n, np.int32)
+    rc = lib().tds_debug_seam_wrap(n, uo.ctypes.data, u.ctypes.data, th.ctypes.data, v.ctypes.data, nw.ctypes.data,
+                                   int(precision))
+    if rc:
+        raise TdsError(rc, "debug seam wrap failed")
+    return u, th, v, nw

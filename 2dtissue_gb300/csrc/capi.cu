@@ -1,0 +1,780 @@
+// C-ABI implementation (include/tds.h): mesh/chart handles, simulation handles, step launch
+// sequencing, CUDA-graph capture of the step loop, state transfer and the device status word.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/tds.h"
+#include "geometry.hpp"
+#include "kernels.cuh"
+#include "mesh.hpp"
+
+using tdsk::R2;
+using tdsk::R4;
+using tdsk::RepParams;
+
+struct tds_mesh {
+    tds::Mesh m;
+    tds::FaceTables t;
+};
+
+namespace {
+
+thread_local std::string g_mesh_err;
+
+int mesh_fail(const std::string& msg) {
+    g_mesh_err = msg;
+    return TDS_ERR_MESH;
+}
+
+int finish_mesh(tds::Mesh& m, tds_mesh** out) {
+    std::string err;
+    if (tds::build_chart(m, err)) return mesh_fail(err);
+    auto* h = new tds_mesh();
+    h->m = std::move(m);
+    tds::build_face_tables(h->m, h->t);
+    *out = h;
+    return TDS_OK;
+}
+
+int ceil_log2(long long x) {
+    int l = 0;
+    while ((1ll << l) < x) ++l;
+    return l;
+}
+
+}  // namespace
+
+struct tds_sim {
+    int precision = 32;
+    int R = 1, N = 0, local_bits = 31;
+    std::vector<int> n_rep, off;
+    std::vector<tds_params> prm;
+    std::vector<tds::Fold> fold;
+    uint64_t seed = 0;
+    long long step = 0;  // completed steps
+    const tds_mesh* mesh = nullptr;
+    std::string err;
+    cudaStream_t stream = nullptr;
+    size_t rsz = 4;  // sizeof(real)
+    // device
+    void* rec = nullptr;
+    int* bin_start = nullptr;
+    int* bin_faces = nullptr;
+    int G = 1;
+    void* reps = nullptr;
+    long long M = 0;
+    int n_tiles = 0;
+    void* pos[2] = {nullptr, nullptr};
+    void* uv[2] = {nullptr, nullptr};
+    int* face[2] = {nullptr, nullptr};
+    int* ids[2] = {nullptr, nullptr};
+    void* vel[2] = {nullptr, nullptr};
+    int* cnt[2] = {nullptr, nullptr};
+    int* key[2] = {nullptr, nullptr};
+    int* rank[2] = {nullptr, nullptr};
+    int* perm = nullptr;
+    int* start = nullptr;
+    int* count = nullptr;
+    unsigned long long* tile_state = nullptr;
+    unsigned* tickets = nullptr;
+    unsigned long long* phi_acc = nullptr;
+    double* series = nullptr;
+    long long series_cap = 0;  // steps
+    int* status = nullptr;
+    long long* d_step = nullptr;
+    int* packed_ids = nullptr;
+    void* noise = nullptr;
+    size_t noise_cap = 0;
+    double* st_d = nullptr;  // staging (double) 8N
+    int* st_i = nullptr;     // staging (int) 2N
+    int cur = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int graph_steps = 16;
+    double origin[3] = {0, 0, 0};
+    std::vector<void*> allocs;
+    // per-kernel event timing
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+    double k_ms[4] = {0, 0, 0, 0};
+    long long k_n[4] = {0, 0, 0, 0};
+};
+
+namespace {
+
+int fail(tds_sim* s, int code, const std::string& msg) {
+    if (s) s->err = msg;
+    return code;
+}
+#define CK(call)                                                                                            \
+    do {                                                                                                    \
+        cudaError_t e_ = (call);                                                                            \
+        if (e_ != cudaSuccess) return fail(s, TDS_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T>
+int dalloc(tds_sim* s, T** p, size_t bytes) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(bytes, 16));
+    if (e != cudaSuccess) return fail(s, TDS_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    s->allocs.push_back(q);
+    *p = (T*)q;
+    return TDS_OK;
+}
+
+void free_graphs(tds_sim* s) {
+    for (auto& g : s->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
+
+template <typename real>
+int upload_tables(tds_sim* s) {
+    const tds::FaceTables& t = s->mesh->t;
+    std::vector<real> rec(t.rec.size());
+    for (size_t i = 0; i < rec.size(); ++i) rec[i] = (real)t.rec[i];
+    int rc;
+    if ((rc = dalloc(s, (real**)&s->rec, rec.size() * sizeof(real)))) return rc;
+    CK(cudaMemcpy(s->rec, rec.data(), rec.size() * sizeof(real), cudaMemcpyHostToDevice));
+    s->G = t.G;
+    if ((rc = dalloc(s, &s->bin_start, t.bin_start.size() * sizeof(int)))) return rc;
+    if ((rc = dalloc(s, &s->bin_faces, t.bin_faces.size() * sizeof(int)))) return rc;
+    CK(cudaMemcpy(s->bin_start, t.bin_start.data(), t.bin_start.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->bin_faces, t.bin_faces.data(), t.bin_faces.size() * sizeof(int), cudaMemcpyHostToDevice));
+
+    // replica table: parameters, fixed-point scales and cell-grid folds
+    std::vector<RepParams<real>> rp(s->R);
+    long long base = 0;
+    double hmax = 0;
+    for (int r = 0; r < s->R; ++r) hmax = std::max(hmax, s->prm[r].r_max);
+    for (int k = 0; k < 3; ++k) s->origin[k] = t.lo[k] - 2.0 * hmax;
+    s->fold.resize(s->R);
+    for (int r = 0; r < s->R; ++r) {
+        const tds_params& p = s->prm[r];
+        RepParams<real>& q = rp[r];
+        std::memset(&q, 0, sizeof q);
+        const double h = p.r_max;
+        q.twoR = (real)(2 * p.radius);
+        q.inv_twoR = (real)(1.0 / (2 * p.radius));
+        q.k = (real)p.k_rep;
+        q.adh_scale = (real)(p.k_adh / (p.r_max - 2 * p.radius));
+        q.r_max2 = (real)(p.r_max * p.r_max);
+        q.v0 = (real)p.v0;
+        q.mu = (real)p.mu;
+        q.inv_tau = (real)(1.0 / p.tau);
+        q.align = (real)p.align;
+        q.eta = (real)p.eta;
+        q.dt = (real)p.dt;
+        q.inv_h = (real)(1.0 / h);
+        const double B = std::max({p.k_rep, p.k_adh, 1e-30});
+        int S = (int)std::floor(52.0 - std::log2(B));
+        S = std::max(0, std::min(S, 60));
+        q.fscale = (real)std::ldexp(1.0, S);
+        q.inv_fscale = (real)std::ldexp(1.0, -S);
+        q.phiscale = std::ldexp(1.0, 62 - ceil_log2((long long)s->n_rep[r] + 1));
+        q.inv_n = 1.0 / std::max(1, s->n_rep[r]);
+        q.force_mode = p.force_mode;
+        tds::Fold fo = tds::choose_fold(s->n_rep[r], t, h);
+        s->fold[r] = fo;
+        q.base = (int)base;
+        q.lx = fo.lx, q.ly = fo.ly, q.lz = fo.lz;
+        q.n = s->n_rep[r];
+        q.off = s->off[r];
+        base += fo.M;
+    }
+    if (base > (1ll << 30)) return fail(s, TDS_ERR_LIMIT, "cell-list buckets exceed 2^30");
+    s->M = base;
+    if ((rc = dalloc(s, (RepParams<real>**)&s->reps, rp.size() * sizeof(RepParams<real>)))) return rc;
+    CK(cudaMemcpy(s->reps, rp.data(), rp.size() * sizeof(RepParams<real>), cudaMemcpyHostToDevice));
+    return TDS_OK;
+}
+
+template <typename real>
+int alloc_state(tds_sim* s) {
+    const size_t N = (size_t)s->N;
+    int rc;
+    for (int b = 0; b < 2; ++b) {
+        if ((rc = dalloc(s, (R4<real>**)&s->pos[b], N * sizeof(R4<real>)))) return rc;
+        if ((rc = dalloc(s, (R2<real>**)&s->uv[b], N * sizeof(R2<real>)))) return rc;
+        if ((rc = dalloc(s, &s->face[b], N * sizeof(int)))) return rc;
+        if ((rc = dalloc(s, &s->ids[b], N * sizeof(int)))) return rc;
+        if ((rc = dalloc(s, (R2<real>**)&s->vel[b], N * sizeof(R2<real>)))) return rc;
+        if ((rc = dalloc(s, &s->cnt[b], N * sizeof(int)))) return rc;
+        if ((rc = dalloc(s, &s->key[b], N * sizeof(int)))) return rc;
+        if ((rc = dalloc(s, &s->rank[b], N * sizeof(int)))) return rc;
+    }
+    if ((rc = dalloc(s, &s->perm, N * sizeof(int)))) return rc;
+    if ((rc = dalloc(s, &s->start, (size_t)(s->M + 1) * sizeof(int)))) return rc;
+    if ((rc = dalloc(s, &s->count, (size_t)s->M * sizeof(int)))) return rc;
+    s->n_tiles = (int)((s->M + tdsk::kScanTile - 1) / tdsk::kScanTile);
+    if ((rc = dalloc(s, &s->tile_state, (size_t)s->n_tiles * sizeof(unsigned long long)))) return rc;
+    if ((rc = dalloc(s, &s->tickets, 2 * sizeof(unsigned)))) return rc;
+    if ((rc = dalloc(s, &s->phi_acc, (size_t)s->R * tdsk::kPhiCopies * 6 * sizeof(unsigned long long)))) return rc;
+    if ((rc = dalloc(s, &s->status, sizeof(int)))) return rc;
+    if ((rc = dalloc(s, &s->d_step, sizeof(long long)))) return rc;
+    if ((rc = dalloc(s, &s->packed_ids, N * sizeof(int)))) return rc;
+    if ((rc = dalloc(s, &s->st_d, 8 * N * sizeof(double)))) return rc;
+    if ((rc = dalloc(s, &s->st_i, 2 * N * sizeof(int)))) return rc;
+    CK(cudaMemset(s->count, 0, (size_t)s->M * sizeof(int)));
+    CK(cudaMemset(s->tile_state, 0, (size_t)s->n_tiles * sizeof(unsigned long long)));
+    CK(cudaMemset(s->tickets, 0, 2 * sizeof(unsigned)));
+    CK(cudaMemset(s->phi_acc, 0, (size_t)s->R * tdsk::kPhiCopies * 6 * sizeof(unsigned long long)));
+    CK(cudaMemset(s->status, 0, sizeof(int)));
+    const int nN = s->N;
+    CK(cudaMemcpy(s->start + s->M, &nN, sizeof(int), cudaMemcpyHostToDevice));
+    const long long m1 = -1;
+    CK(cudaMemcpy(s->d_step, &m1, sizeof m1, cudaMemcpyHostToDevice));
+    std::vector<int> pid(N);
+    for (int r = 0; r < s->R; ++r)
+        for (int i = 0; i < s->n_rep[r]; ++i) pid[s->off[r] + i] = (int)(((unsigned)r << s->local_bits) | (unsigned)i);
+    CK(cudaMemcpy(s->packed_ids, pid.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    return TDS_OK;
+}
+
+int ensure_series(tds_sim* s, long long steps_needed) {
+    if (steps_needed <= s->series_cap) return TDS_OK;
+    long long cap = std::max<long long>(1024, s->series_cap);
+    while (cap < steps_needed) cap *= 2;
+    double* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, (size_t)cap * 2 * s->R * sizeof(double));
+    if (e != cudaSuccess) return fail(s, TDS_ERR_NOMEM, "order-parameter series allocation failed");
+    CK(cudaMemsetAsync(p, 0, (size_t)cap * 2 * s->R * sizeof(double), s->stream));
+    if (s->series) {
+        CK(cudaMemcpyAsync(p, s->series, (size_t)s->series_cap * 2 * s->R * sizeof(double), cudaMemcpyDeviceToDevice,
+                           s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        cudaFree(s->series);
+    }
+    s->series = p;
+    s->series_cap = cap;
+    free_graphs(s);
+    return TDS_OK;
+}
+
+cudaEvent_t take_event(tds_sim* s) {
+    if (s->ev_pool.empty()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+    cudaEvent_t e = s->ev_pool.back();
+    s->ev_pool.pop_back();
+    return e;
+}
+
+// Records an event pair around kernel `k` when timing is enabled.
+struct KernelTimer {
+    tds_sim* s;
+    int k;
+    cudaEvent_t a = nullptr;
+    KernelTimer(tds_sim* s_, int k_) : s(s_), k(k_) {
+        if (s->timing) {
+            a = take_event(s);
+            cudaEventRecord(a, s->stream);
+        }
+    }
+    ~KernelTimer() {
+        if (s->timing) {
+            cudaEvent_t b = take_event(s);
+            cudaEventRecord(b, s->stream);
+            s->ev_pending.push_back({k, {a, b}});
+        }
+    }
+};
+
+void collect_times(tds_sim* s) {
+    if (s->ev_pending.empty()) return;
+    cudaStreamSynchronize(s->stream);
+    for (auto& p : s->ev_pending) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+        s->k_ms[p.first] += ms;
+        s->k_n[p.first] += 1;
+        s->ev_pool.push_back(p.second.first);
+        s->ev_pool.push_back(p.second.second);
+    }
+    s->ev_pending.clear();
+}
+
+template <typename real>
+void launch_one_step(tds_sim* s, const real* noise) {
+    const int c = s->cur, o = c ^ 1;
+    cudaStream_t st = s->stream;
+    {
+        KernelTimer kt(s, 0);
+        tdsk::k_scan<<<s->n_tiles, tdsk::kScanThreads, 0, st>>>(s->count, s->start, s->M, s->tile_state,
+                                                                 s->tickets, s->d_step, s->status);
+    }
+    const int nb = (s->N + 255) / 256;
+    {
+        KernelTimer kt(s, 1);
+        tdsk::k_scatter<<<nb, 256, 0, st>>>(s->key[c], s->rank[c], s->start, s->perm, s->N, s->d_step);
+    }
+    tdsk::StepArgs<real> a;
+    a.pos = (const R4<real>*)s->pos[c];
+    a.uv = (const R2<real>*)s->uv[c];
+    a.face = s->face[c];
+    a.ids = s->ids[c];
+    a.pos_o = (R4<real>*)s->pos[o];
+    a.uv_o = (R2<real>*)s->uv[o];
+    a.face_o = s->face[o];
+    a.ids_o = s->ids[o];
+    a.vel_o = (R2<real>*)s->vel[o];
+    a.cnt_o = s->cnt[o];
+    a.key_o = s->key[o];
+    a.rank_o = s->rank[o];
+    a.perm = s->perm;
+    a.start = s->start;
+    a.count = s->count;
+    a.rec = (const real*)s->rec;
+    a.G = s->G;
+    a.bin_start = s->bin_start;
+    a.bin_faces = s->bin_faces;
+    a.reps = (const RepParams<real>*)s->reps;
+    a.local_bits = s->local_bits;
+    a.ox = (real)s->origin[0], a.oy = (real)s->origin[1], a.oz = (real)s->origin[2];
+    a.cx = (real)s->mesh->t.centroid[0], a.cy = (real)s->mesh->t.centroid[1], a.cz = (real)s->mesh->t.centroid[2];
+    a.noise = noise;
+    a.phi_acc = s->phi_acc;
+    a.d_step = s->d_step;
+    a.seed = s->seed;
+    a.status = s->status;
+    a.N = s->N;
+    const int ns = (s->N + tdsk::kStepThreads - 1) / tdsk::kStepThreads;
+    {
+        KernelTimer kt(s, 2);
+        tdsk::k_step<real><<<ns, tdsk::kStepThreads, 0, st>>>(a);
+    }
+    {
+        KernelTimer kt(s, 3);
+        tdsk::k_finalize<real><<<(s->R + 127) / 128, 128, 0, st>>>(
+            s->phi_acc, (const RepParams<real>*)s->reps, s->R, s->series, 0, s->series_cap, s->d_step);
+    }
+    s->cur = o;
+}
+
+template <typename real>
+int run_steps(tds_sim* s, int n, const double* noise_host, bool sync = true) {
+    int rc;
+    if ((rc = ensure_series(s, s->step + n))) return rc;
+    if (noise_host) {
+        const size_t N = (size_t)s->N;
+        if (s->noise_cap < N) {
+            if (s->noise) cudaFree(s->noise);
+            s->noise = nullptr;
+            CK(cudaMalloc(&s->noise, N * sizeof(real)));
+            s->noise_cap = N;
+        }
+        std::vector<real> tmp(N);
+        for (int k = 0; k < n; ++k) {
+            for (size_t i = 0; i < N; ++i) tmp[i] = (real)noise_host[(size_t)k * N + i];
+            CK(cudaMemcpyAsync(s->noise, tmp.data(), N * sizeof(real), cudaMemcpyHostToDevice, s->stream));
+            launch_one_step<real>(s, (const real*)s->noise);
+            CK(cudaStreamSynchronize(s->stream));
+        }
+    } else {
+        int left = n;
+        while (!s->timing && left >= s->graph_steps) {
+            const int c = s->cur;
+            if (!s->graph[c]) {
+                cudaGraph_t g;
+                CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+                for (int k = 0; k < s->graph_steps; ++k) launch_one_step<real>(s, nullptr);
+                CK(cudaStreamEndCapture(s->stream, &g));
+                s->cur = c;  // capture recorded the launches; the state did not advance
+                CK(cudaGraphInstantiate(&s->graph[c], g, 0));
+                cudaGraphDestroy(g);
+            }
+            CK(cudaGraphLaunch(s->graph[c], s->stream));
+            // graph_steps is even: the current buffer is the same after the chunk
+            left -= s->graph_steps;
+        }
+        for (int k = 0; k < left; ++k) launch_one_step<real>(s, nullptr);
+        CK(cudaGetLastError());
+    }
+    s->step += n;
+    if (!sync) return TDS_OK;
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (st) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "device status 0x%x after step %lld (1 non-finite, 2 wrap limit, 4 locate "
+                      "fallback, 8 neighbour overflow, 32 scan timeout)", st, s->step);
+        return fail(s, TDS_ERR_STATE, buf);
+    }
+    return TDS_OK;
+}
+
+template <typename real>
+int load_state(tds_sim* s, const tds_state_view* in) {
+    const size_t N = (size_t)s->N;
+    if (!in || !in->uv || !in->theta) return fail(s, TDS_ERR_ARG, "set_state needs uv and theta");
+    if (in->face)
+        for (size_t i = 0; i < N; ++i)
+            if (in->face[i] >= s->mesh->t.F) return fail(s, TDS_ERR_ARG, "set_state: face index out of range");
+    double* d_uv = s->st_d;
+    double* d_th = s->st_d + 2 * N;
+    double* d_r3 = s->st_d + 3 * N;
+    int* d_face = s->st_i;
+    CK(cudaMemcpyAsync(d_uv, in->uv, 2 * N * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(d_th, in->theta, N * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    if (in->face) CK(cudaMemcpyAsync(d_face, in->face, N * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    if (in->r3d) CK(cudaMemcpyAsync(d_r3, in->r3d, 3 * N * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    s->cur = 0;
+    const int nb = (s->N + 255) / 256;
+    tdsk::k_load_state<real><<<nb, 256, 0, s->stream>>>(
+        d_uv, d_th, d_face, d_r3, in->face != nullptr, in->r3d != nullptr, (const real*)s->rec, s->G, s->bin_start,
+        s->bin_faces, s->packed_ids, (R4<real>*)s->pos[0], (R2<real>*)s->uv[0], s->face[0], s->ids[0],
+        (R2<real>*)s->vel[0], s->cnt[0], s->N, s->status);
+    CK(cudaMemsetAsync(s->count, 0, (size_t)s->M * sizeof(int), s->stream));
+    tdsk::k_prime<real><<<nb, 256, 0, s->stream>>>((const R4<real>*)s->pos[0], s->ids[0],
+                                                    (const RepParams<real>*)s->reps, s->local_bits,
+                                                    (real)s->origin[0], (real)s->origin[1], (real)s->origin[2],
+                                                    s->count, s->key[0], s->rank[0], s->N);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    return TDS_OK;
+}
+
+template <typename real>
+int save_state(tds_sim* s, tds_state_view* out) {
+    const size_t N = (size_t)s->N;
+    double* d_uv = s->st_d;
+    double* d_th = s->st_d + 2 * N;
+    double* d_r3 = s->st_d + 3 * N;
+    double* d_vel = s->st_d + 6 * N;
+    int* d_face = s->st_i;
+    int* d_cnt = s->st_i + N;
+    const int c = s->cur;
+    const int nb = (s->N + 255) / 256;
+    tdsk::k_gather_state<real><<<nb, 256, 0, s->stream>>>(
+        (const R4<real>*)s->pos[c], (const R2<real>*)s->uv[c], s->face[c], s->ids[c], (const R2<real>*)s->vel[c],
+        s->cnt[c], (const RepParams<real>*)s->reps, s->local_bits, d_uv, d_th, d_face, d_r3, d_vel, d_cnt, s->N);
+    CK(cudaGetLastError());
+    if (out->uv) CK(cudaMemcpyAsync(out->uv, d_uv, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    if (out->theta) CK(cudaMemcpyAsync(out->theta, d_th, N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    if (out->face) CK(cudaMemcpyAsync(out->face, d_face, N * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    if (out->r3d) CK(cudaMemcpyAsync(out->r3d, d_r3, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    if (out->vel_uv) CK(cudaMemcpyAsync(out->vel_uv, d_vel, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    if (out->nbr_count) CK(cudaMemcpyAsync(out->nbr_count, d_cnt, N * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return TDS_OK;
+}
+
+int check_params(const tds_params& p, std::string& why) {
+    if (!(p.radius > 0)) return why = "radius must be > 0", 1;
+    if (!(p.r_max > 2 * p.radius)) return why = "r_max must exceed 2*radius", 1;
+    if (!(p.tau > 0)) return why = "tau must be > 0", 1;
+    if (!(p.dt > 0)) return why = "dt must be > 0", 1;
+    if (!(p.k_rep >= 0 && p.k_adh >= 0)) return why = "stiffnesses must be >= 0", 1;
+    if (p.force_mode != 0 && p.force_mode != 1) return why = "force_mode must be 0 or 1", 1;
+    return 0;
+}
+
+int create_impl(const tds_mesh* mesh, int R, const int* n, const tds_params* prm, uint64_t seed, int precision,
+                tds_sim** out) {
+    if (!out) return TDS_ERR_ARG;
+    *out = nullptr;
+    auto s = std::make_unique<tds_sim>();
+    if (!mesh) return fail(nullptr, TDS_ERR_ARG, "");
+    if (precision != 32 && precision != 64) return TDS_ERR_ARG;
+    if (R < 1) return TDS_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return TDS_ERR_CUDA;
+    s->mesh = mesh;
+    s->precision = precision;
+    s->rsz = precision == 32 ? 4 : 8;
+    s->R = R;
+    s->seed = seed;
+    long long total = 0;
+    int nmax = 0;
+    for (int r = 0; r < R; ++r) {
+        std::string why;
+        if (n[r] < 1 || check_params(prm[r], why)) return TDS_ERR_ARG;
+        s->off.push_back((int)total);
+        s->n_rep.push_back(n[r]);
+        s->prm.push_back(prm[r]);
+        total += n[r];
+        nmax = std::max(nmax, n[r]);
+    }
+    if (total > (1ll << 30)) return TDS_ERR_LIMIT;
+    s->N = (int)total;
+    s->local_bits = R == 1 ? 31 : std::max(1, ceil_log2(nmax));
+    if (R > 1 && ceil_log2(R) + s->local_bits > 31) return TDS_ERR_LIMIT;
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return TDS_ERR_CUDA;
+    tds_sim* sp = s.get();
+    int rc = precision == 32 ? upload_tables<float>(sp) : upload_tables<double>(sp);
+    if (!rc) rc = precision == 32 ? alloc_state<float>(sp) : alloc_state<double>(sp);
+    if (!rc) rc = ensure_series(sp, 1024);
+    if (rc) {
+        tds_destroy(s.release());
+        return rc;
+    }
+    *out = s.release();
+    return TDS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---------------------------------------------------------------------------------------------
+// mesh
+// ---------------------------------------------------------------------------------------------
+int tds_mesh_ellipsoid(int level, double ax, double ay, double az, tds_mesh** out) {
+    if (!out || level < 0 || level > 9 || !(ax > 0 && ay > 0 && az > 0)) return mesh_fail("bad arguments"), TDS_ERR_ARG;
+    tds::Mesh m;
+    tds::make_icosphere(level, m);
+    tds::scale_axes(m, ax, ay, az);
+    return finish_mesh(m, out);
+}
+
+int tds_mesh_bumpy_sphere(int level, double amp, double scale, tds_mesh** out) {
+    if (!out || level < 0 || level > 9 || !(scale > 0) || !(std::fabs(amp) < 1))
+        return mesh_fail("bad arguments"), TDS_ERR_ARG;
+    tds::Mesh m;
+    tds::make_icosphere(level, m);
+    tds::bumpy_sphere(m, amp, scale);
+    tds::orient_outward(m);
+    return finish_mesh(m, out);
+}
+
+int tds_mesh_from_arrays(const double* v3, int V, const int* f3, int F, tds_mesh** out) {
+    if (!out || !v3 || !f3 || V < 4 || F < 4) return mesh_fail("bad arguments"), TDS_ERR_ARG;
+    tds::Mesh m;
+    m.v3.assign(v3, v3 + 3 * (size_t)V);
+    m.f3.assign(f3, f3 + 3 * (size_t)F);
+    for (int i = 0; i < 3 * F; ++i)
+        if (m.f3[i] < 0 || m.f3[i] >= V) return mesh_fail("face index out of range"), TDS_ERR_ARG;
+    tds::orient_outward(m);
+    return finish_mesh(m, out);
+}
+
+int tds_mesh_load_off(const char* path, tds_mesh** out) {
+    if (!out || !path) return mesh_fail("bad arguments"), TDS_ERR_ARG;
+    tds::Mesh m;
+    std::string err;
+    if (tds::read_off(path, m, err)) return mesh_fail(err);
+    tds::orient_outward(m);
+    return finish_mesh(m, out);
+}
+
+int tds_mesh_save_off(const tds_mesh* h, const char* path) {
+    if (!h || !path) return TDS_ERR_ARG;
+    std::string err;
+    if (tds::write_off(path, h->m, err)) return mesh_fail(err);
+    return TDS_OK;
+}
+
+int tds_mesh_info(const tds_mesh* h, int* V, int* F, int* Vuv, double* area) {
+    if (!h) return TDS_ERR_ARG;
+    if (V) *V = h->m.V();
+    if (F) *F = h->m.F();
+    if (Vuv) *Vuv = h->m.Vuv();
+    if (area) *area = h->t.area;
+    return TDS_OK;
+}
+
+int tds_mesh_arrays(const tds_mesh* h, double* v3, int* f3, double* uv, int* fuv, int* uv2v) {
+    if (!h) return TDS_ERR_ARG;
+    const tds::Mesh& m = h->m;
+    if (v3) std::memcpy(v3, m.v3.data(), m.v3.size() * sizeof(double));
+    if (f3) std::memcpy(f3, m.f3.data(), m.f3.size() * sizeof(int));
+    if (uv) std::memcpy(uv, m.uv.data(), m.uv.size() * sizeof(double));
+    if (fuv) std::memcpy(fuv, m.fuv.data(), m.fuv.size() * sizeof(int));
+    if (uv2v) std::memcpy(uv2v, m.uv2v.data(), m.uv2v.size() * sizeof(int));
+    return TDS_OK;
+}
+
+void tds_mesh_destroy(tds_mesh* h) { delete h; }
+
+const char* tds_mesh_last_error(void) { return g_mesh_err.c_str(); }
+
+// ---------------------------------------------------------------------------------------------
+// simulation
+// ---------------------------------------------------------------------------------------------
+int tds_create(const tds_mesh* mesh, const tds_params* params, int n_particles, uint64_t seed, int precision,
+               tds_sim** out) {
+    if (!params) return TDS_ERR_ARG;
+    return create_impl(mesh, 1, &n_particles, params, seed, precision, out);
+}
+
+int tds_ensemble_create(const tds_mesh* mesh, int n_replicas, const int* n_particles, const tds_params* params,
+                        uint64_t seed, int precision, tds_sim** out) {
+    if (!n_particles || !params) return TDS_ERR_ARG;
+    return create_impl(mesh, n_replicas, n_particles, params, seed, precision, out);
+}
+
+int tds_start(tds_sim* s) {
+    if (!s) return TDS_ERR_ARG;
+    const size_t N = (size_t)s->N;
+    std::vector<double> uv(2 * N), th(N), r3(3 * N);
+    std::vector<int> fc(N);
+    for (int r = 0; r < s->R; ++r) {
+        const size_t o = (size_t)s->off[r];
+        tds::init_particles(s->mesh->m, s->mesh->t, s->n_rep[r], s->seed, (uint32_t)r, &uv[2 * o], &th[o], &fc[o],
+                            &r3[3 * o]);
+    }
+    tds_state_view v{uv.data(), th.data(), fc.data(), r3.data(), nullptr, nullptr};
+    return tds_set_state(s, &v);
+}
+
+int tds_step(tds_sim* s, int n_steps, const double* noise) {
+    if (!s || n_steps < 0) return TDS_ERR_ARG;
+    if (n_steps == 0) return TDS_OK;
+    return s->precision == 32 ? run_steps<float>(s, n_steps, noise) : run_steps<double>(s, n_steps, noise);
+}
+
+int tds_step_async(tds_sim* s, int n_steps) {
+    if (!s || n_steps < 0) return TDS_ERR_ARG;
+    if (n_steps == 0) return TDS_OK;
+    return s->precision == 32 ? run_steps<float>(s, n_steps, nullptr, false)
+                              : run_steps<double>(s, n_steps, nullptr, false);
+}
+
+int tds_kernel_timing(tds_sim* s, int enable) {
+    if (!s) return TDS_ERR_ARG;
+    collect_times(s);
+    s->timing = enable != 0;
+    for (int k = 0; k < 4; ++k) s->k_ms[k] = 0, s->k_n[k] = 0;
+    return TDS_OK;
+}
+
+int tds_kernel_times(tds_sim* s, double* total_ms, long long* launches) {
+    if (!s) return TDS_ERR_ARG;
+    collect_times(s);
+    for (int k = 0; k < 4; ++k) {
+        if (total_ms) total_ms[k] = s->k_ms[k];
+        if (launches) launches[k] = s->k_n[k];
+    }
+    return TDS_OK;
+}
+
+int tds_update(tds_sim* s, tds_state_view* out) {
+    int rc = tds_step(s, 1, nullptr);
+    if (rc) return rc;
+    return out ? tds_get_state(s, out) : TDS_OK;
+}
+
+int tds_set_state(tds_sim* s, const tds_state_view* in) {
+    if (!s) return TDS_ERR_ARG;
+    return s->precision == 32 ? load_state<float>(s, in) : load_state<double>(s, in);
+}
+
+int tds_get_state(tds_sim* s, tds_state_view* out) {
+    if (!s || !out) return TDS_ERR_ARG;
+    return s->precision == 32 ? save_state<float>(s, out) : save_state<double>(s, out);
+}
+
+int tds_get_order_parameter(tds_sim* s, double* phi, double* psi, int cap, int* n_steps) {
+    if (!s) return TDS_ERR_ARG;
+    const long long n = std::min<long long>(s->step, s->series_cap);
+    if (n_steps) *n_steps = (int)n;
+    if (n == 0 || cap <= 0) return TDS_OK;
+    std::vector<double> tmp((size_t)n * 2 * s->R);
+    CK(cudaMemcpyAsync(tmp.data(), s->series, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    const long long m = std::min<long long>((long long)cap, n * s->R);
+    for (long long k = 0; k < m; ++k) {
+        const long long t = k / s->R, r = k % s->R;
+        if (phi) phi[k] = tmp[(size_t)t * 2 * s->R + r];
+        if (psi) psi[k] = tmp[(size_t)t * 2 * s->R + s->R + r];
+    }
+    return TDS_OK;
+}
+
+int tds_get_step(const tds_sim* s, int64_t* step) {
+    if (!s || !step) return TDS_ERR_ARG;
+    *step = s->step;
+    return TDS_OK;
+}
+
+int tds_get_status(tds_sim* s, int* status) {
+    if (!s || !status) return TDS_ERR_ARG;
+    CK(cudaMemcpyAsync(status, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return TDS_OK;
+}
+
+int tds_clear_status(tds_sim* s) {
+    if (!s) return TDS_ERR_ARG;
+    CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return TDS_OK;
+}
+
+int tds_num_particles(const tds_sim* s, int* n_total, int* n_replicas) {
+    if (!s) return TDS_ERR_ARG;
+    if (n_total) *n_total = s->N;
+    if (n_replicas) *n_replicas = s->R;
+    return TDS_OK;
+}
+
+int tds_stream(tds_sim* s, void** stream) {
+    if (!s || !stream) return TDS_ERR_ARG;
+    *stream = (void*)s->stream;
+    return TDS_OK;
+}
+
+int tds_kernels_per_step(const tds_sim* s, int* n) {
+    if (!s || !n) return TDS_ERR_ARG;
+    *n = 4;
+    return TDS_OK;
+}
+
+const char* tds_last_error(const tds_sim* s) { return s ? s->err.c_str() : "null handle"; }
+
+void tds_destroy(tds_sim* s) {
+    if (!s) return;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    collect_times(s);
+    for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
+    free_graphs(s);
+    for (void* p : s->allocs) cudaFree(p);
+    if (s->series) cudaFree(s->series);
+    if (s->noise) cudaFree(s->noise);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+int tds_debug_seam_wrap(int n, const double* uv_old, double* uv, double* theta, double* vel_uv, int* n_wraps,
+                        int precision) {
+    tds_sim* s = nullptr;
+    if (n <= 0 || !uv_old || !uv) return TDS_ERR_ARG;
+    double *d_old = nullptr, *d_uv = nullptr, *d_th = nullptr, *d_vel = nullptr;
+    int* d_nw = nullptr;
+    CK(cudaMalloc(&d_old, 2 * n * sizeof(double)));
+    CK(cudaMalloc(&d_uv, 2 * n * sizeof(double)));
+    CK(cudaMalloc(&d_th, n * sizeof(double)));
+    CK(cudaMalloc(&d_vel, 2 * n * sizeof(double)));
+    CK(cudaMalloc(&d_nw, n * sizeof(int)));
+    CK(cudaMemcpy(d_old, uv_old, 2 * n * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_uv, uv, 2 * n * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemset(d_th, 0, n * sizeof(double)));
+    CK(cudaMemset(d_vel, 0, 2 * n * sizeof(double)));
+    if (theta) CK(cudaMemcpy(d_th, theta, n * sizeof(double), cudaMemcpyHostToDevice));
+    if (vel_uv) CK(cudaMemcpy(d_vel, vel_uv, 2 * n * sizeof(double), cudaMemcpyHostToDevice));
+    if (precision == 64)
+        tdsk::k_debug_wrap<double><<<(n + 127) / 128, 128>>>(n, d_old, d_uv, d_th, d_vel, d_nw);
+    else
+        tdsk::k_debug_wrap<float><<<(n + 127) / 128, 128>>>(n, d_old, d_uv, d_th, d_vel, d_nw);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(uv, d_uv, 2 * n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (theta) CK(cudaMemcpy(theta, d_th, n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (vel_uv) CK(cudaMemcpy(vel_uv, d_vel, 2 * n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (n_wraps) CK(cudaMemcpy(n_wraps, d_nw, n * sizeof(int), cudaMemcpyDeviceToHost));
+    cudaFree(d_old), cudaFree(d_uv), cudaFree(d_th), cudaFree(d_vel), cudaFree(d_nw);
+    return TDS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,176 @@
+#include "geometry.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "philox.cuh"
+
+namespace tds {
+
+void philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    tdsr::philox10(ctr, key, out);
+}
+
+void build_face_tables(const Mesh& m, FaceTables& t) {
+    const int F = m.F();
+    t.F = F;
+    t.rec.assign((size_t)F * kFaceRec, 0.0);
+    t.area_cdf.assign(F, 0.0);
+    double acc = 0;
+    for (int f = 0; f < F; ++f) {
+        double* r = &t.rec[(size_t)f * kFaceRec];
+        const int* tu = &m.fuv[3 * f];
+        const int* t3 = &m.f3[3 * f];
+        double a[2], b[2], c[2], A[3], B[3], C[3];
+        for (int k = 0; k < 2; ++k) a[k] = m.uv[2 * tu[0] + k], b[k] = m.uv[2 * tu[1] + k], c[k] = m.uv[2 * tu[2] + k];
+        for (int k = 0; k < 3; ++k) A[k] = m.v3[3 * t3[0] + k], B[k] = m.v3[3 * t3[1] + k], C[k] = m.v3[3 * t3[2] + k];
+        const double m00 = b[0] - a[0], m01 = c[0] - a[0], m10 = b[1] - a[1], m11 = c[1] - a[1];
+        const double det = m00 * m11 - m01 * m10;
+        const double i00 = m11 / det, i01 = -m01 / det, i10 = -m10 / det, i11 = m00 / det;
+        double E0[3], E1[3];
+        for (int k = 0; k < 3; ++k) E0[k] = B[k] - A[k], E1[k] = C[k] - A[k];
+        double J[6];
+        for (int k = 0; k < 3; ++k) {
+            J[k] = E0[k] * i00 + E1[k] * i10;
+            J[3 + k] = E0[k] * i01 + E1[k] * i11;
+        }
+        const double a11 = J[0] * J[0] + J[1] * J[1] + J[2] * J[2];
+        const double a12 = J[0] * J[3] + J[1] * J[4] + J[2] * J[5];
+        const double a22 = J[3] * J[3] + J[4] * J[4] + J[5] * J[5];
+        const double dd = a11 * a22 - a12 * a12;
+        const double b11 = a22 / dd, b12 = -a12 / dd, b22 = a11 / dd;
+        for (int k = 0; k < 6; ++k) r[k] = J[k];
+        for (int k = 0; k < 3; ++k) {
+            r[6 + k] = b11 * J[k] + b12 * J[3 + k];
+            r[9 + k] = b12 * J[k] + b22 * J[3 + k];
+        }
+        const double nx = E0[1] * E1[2] - E0[2] * E1[1], ny = E0[2] * E1[0] - E0[0] * E1[2],
+                     nz = E0[0] * E1[1] - E0[1] * E1[0];
+        const double nn = std::sqrt(nx * nx + ny * ny + nz * nz);
+        r[12] = nx / nn, r[13] = ny / nn, r[14] = nz / nn;
+        r[16] = a[0], r[17] = a[1], r[18] = b[0], r[19] = b[1], r[20] = c[0], r[21] = c[1];
+        r[22] = A[0], r[23] = A[1], r[24] = A[2];
+        const double* P[3] = {a, b, c};
+        int bits = 0;
+        for (int k = 0; k < 3; ++k) {
+            const double ex = P[(k + 1) % 3][0] - P[k][0], ey = P[(k + 1) % 3][1] - P[k][1];
+            r[25 + k] = 1.0 / std::sqrt(ex * ex + ey * ey);
+            if (tu[k] > tu[(k + 1) % 3]) bits |= 1 << k;
+        }
+        r[28] = (double)bits;
+        acc += 0.5 * nn;
+        t.area_cdf[f] = acc;
+    }
+    t.area = acc;
+    for (int f = 0; f < F; ++f) t.area_cdf[f] /= acc;
+    t.area_cdf[F - 1] = 1.0;
+
+    // UV bins: closed bounding boxes widened by 1e-6 so that an FP32 bin assignment of a point
+    // on a bin border still finds every face that contains it.
+    int G = (int)std::ceil(std::sqrt((double)F));
+    G = std::max(1, std::min(G, 4096));
+    t.G = G;
+    auto bc = [G](double x) {
+        int v = (int)std::floor(x * G);
+        return v < 0 ? 0 : (v >= G ? G - 1 : v);
+    };
+    const double eps = 1e-6;
+    std::vector<int> cnt((size_t)G * G + 1, 0);
+    auto box = [&](int f, int& x0, int& x1, int& y0, int& y1) {
+        const double* r = &t.rec[(size_t)f * kFaceRec];
+        double xmn = std::min(r[16], std::min(r[18], r[20])), xmx = std::max(r[16], std::max(r[18], r[20]));
+        double ymn = std::min(r[17], std::min(r[19], r[21])), ymx = std::max(r[17], std::max(r[19], r[21]));
+        x0 = bc(xmn - eps), x1 = bc(xmx + eps), y0 = bc(ymn - eps), y1 = bc(ymx + eps);
+    };
+    for (int f = 0; f < F; ++f) {
+        int x0, x1, y0, y1;
+        box(f, x0, x1, y0, y1);
+        for (int y = y0; y <= y1; ++y)
+            for (int x = x0; x <= x1; ++x) cnt[(size_t)y * G + x + 1]++;
+    }
+    for (size_t i = 1; i < cnt.size(); ++i) cnt[i] += cnt[i - 1];
+    t.bin_start = cnt;
+    t.bin_faces.assign(cnt.back(), 0);
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int f = 0; f < F; ++f) {
+        int x0, x1, y0, y1;
+        box(f, x0, x1, y0, y1);
+        for (int y = y0; y <= y1; ++y)
+            for (int x = x0; x <= x1; ++x) t.bin_faces[fill[(size_t)y * G + x]++] = f;
+    }
+
+    for (int k = 0; k < 3; ++k) t.lo[k] = 1e300, t.hi[k] = -1e300, t.centroid[k] = 0;
+    for (int i = 0; i < m.V(); ++i)
+        for (int k = 0; k < 3; ++k) {
+            t.lo[k] = std::min(t.lo[k], m.v3[3 * i + k]);
+            t.hi[k] = std::max(t.hi[k], m.v3[3 * i + k]);
+            t.centroid[k] += m.v3[3 * i + k];
+        }
+    for (int k = 0; k < 3; ++k) t.centroid[k] /= m.V();
+}
+
+static int ceil_log2(int64_t x) {
+    int l = 0;
+    while (((int64_t)1 << l) < x) ++l;
+    return l;
+}
+
+Fold choose_fold(int n, const FaceTables& t, double h) {
+    Fold fo;
+    int L = std::max(6, ceil_log2(2 * (int64_t)std::max(n, 1)));
+    int g[3];
+    for (int k = 0; k < 3; ++k) g[k] = (int)std::ceil((t.hi[k] - t.lo[k]) / h) + 5;
+    // Largest axis first, each fold at least 4 (distinct buckets for a 3-cell run).
+    int lx = std::min(ceil_log2(g[0]), L - 4);
+    lx = std::max(lx, 2);
+    int ly = std::min(ceil_log2(g[1]), L - lx - 2);
+    ly = std::max(ly, 2);
+    int lz = std::max(2, L - lx - ly);
+    fo.lx = lx, fo.ly = ly, fo.lz = lz;
+    fo.M = (int64_t)1 << (lx + ly + lz);
+    return fo;
+}
+
+void init_particles(const Mesh& m, const FaceTables& t, int n, uint64_t seed, uint32_t rep, double* uv,
+                    double* theta, int* face, double* r3d) {
+    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    for (int i = 0; i < n; ++i) {
+        const uint32_t ctr[4] = {(uint32_t)i, rep, 0xFFFFFFFFu, 0u};
+        uint32_t o[4];
+        tdsr::philox10(ctr, key, o);
+        const double u1 = ((double)(o[0] >> 11) + 0.5) * (1.0 / 2097152.0);  // (0,1)
+        const double u2 = (double)(o[1] >> 8) * (1.0 / 16777216.0);
+        const double u3 = (double)(o[2] >> 8) * (1.0 / 16777216.0);
+        const double u4 = (double)(o[3] >> 8) * (1.0 / 16777216.0);
+        int f = (int)(std::lower_bound(t.area_cdf.begin(), t.area_cdf.end(), u1) - t.area_cdf.begin());
+        f = std::min(f, t.F - 1);
+        const double* r = &t.rec[(size_t)f * kFaceRec];
+        const double s2 = std::sqrt(u2);
+        const double w0 = 1.0 - s2, w1 = s2 * (1.0 - u3), w2 = s2 * u3;
+        double pu = w0 * r[16] + w1 * r[18] + w2 * r[20];
+        double pv = w0 * r[17] + w1 * r[19] + w2 * r[21];
+        uv[2 * i] = pu, uv[2 * i + 1] = pv;
+        face[i] = f;
+        const double du = pu - r[16], dv = pv - r[17];
+        for (int k = 0; k < 3; ++k) r3d[3 * i + k] = r[22 + k] + r[k] * du + r[3 + k] * dv;
+        // face frame: e1 along B - A, e2 = n x e1
+        const int* t3 = &m.f3[3 * f];
+        double e1[3], nrm = 0;
+        for (int k = 0; k < 3; ++k) e1[k] = m.v3[3 * t3[1] + k] - m.v3[3 * t3[0] + k], nrm += e1[k] * e1[k];
+        nrm = std::sqrt(nrm);
+        for (int k = 0; k < 3; ++k) e1[k] /= nrm;
+        const double* nn = &r[12];
+        const double e2[3] = {nn[1] * e1[2] - nn[2] * e1[1], nn[2] * e1[0] - nn[0] * e1[2],
+                              nn[0] * e1[1] - nn[1] * e1[0]};
+        const double phi = 6.28318530717958647692 * u4;
+        const double cp = std::cos(phi), sp = std::sin(phi);
+        double p[3];
+        for (int k = 0; k < 3; ++k) p[k] = cp * e1[k] + sp * e2[k];
+        const double w_u = r[6] * p[0] + r[7] * p[1] + r[8] * p[2];
+        const double w_v = r[9] * p[0] + r[10] * p[1] + r[11] * p[2];
+        theta[i] = std::atan2(w_v, w_u);
+    }
+}
+
+}  // namespace tds

@@ -1,0 +1,345 @@
+#!/usr/bin/env python
+"""Throughput of the per-step particle update on one GB300 (and N independent replicas on N GPUs).
+
+Workload (the headline configuration): the (20,10,10) ellipsoid meshed as a level-7 icosphere
+(163,842 vertices, 327,680 faces), 1,048,576 particles at area packing 0.5 (radius from packing,
+r_max = 2.4 R), eta = 0.3, dt = 0.01, FP32 state. Synthetic, seeded placement (no dataset exists).
+
+One bench step = one simulation step of the whole system (4 kernels). L2 is flushed (a 256 MB
+write, outside the timed window) before every timed step; each step is timed with CUDA events on
+the handle's stream. value = particle-steps/s over all ranks (max time over ranks).
+e2e = the same metric through the C-ABI with host buffers: set_state (H2D) + tds_step + get_state
+(D2H) per step, from/to pinned host memory.
+
+--impl reference times the CPU restatement of the path (oracle, FP64, all host threads) on the same
+workload; under torchrun only rank 0 runs it.
+"""
+import argparse
+import importlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s (forward step, 1M-particle plain system)"
+UNIT = "particle-steps/s"
+ALG_BYTES_PARTICLE = 68  # FP32: read uv 8 + theta 4 + face 4 + r3d 12; write those + vel_uv 8 + count 4
+ALG_BYTES_FACE = 60      # 3 UV corners x 8 + 3 3D corners x 12
+ALG_BYTES_REPLICA = 4    # order parameter
+KERNELS_PER_STEP = 4
+
+
+def config2(tg):
+    mesh = tg.Mesh.ellipsoid(7, (20.0, 10.0, 10.0))
+    n = 1 << 20
+    radius = float(np.sqrt(0.5 * mesh.area / (np.pi * n)))
+    p = tg.Params(radius=radius, r_max=2.4 * radius, eta=0.3, dt=0.01)
+    return mesh, p, n
+
+
+def workload_config(mesh, p, n, flush):
+    return {"workload": "plain step, (20,10,10) ellipsoid L7 icosphere, 1,048,576 particles, packing 0.5",
+            "faces": mesh.F, "particles": n, "radius": round(p.radius, 6), "r_max": round(p.r_max, 6),
+            "eta": p.eta, "dt": p.dt, "state": "fp32 SoA", "l2": flush, "seeded": True}
+
+
+def measured_peak():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(n_particles):
+    """DRAM bytes per k_step launch from the committed ncu summary (scaled to n_particles)."""
+    path = os.path.join(ROOT, "profiles", "k_step_config2.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_particle:"):
+                return float(line.split(":")[1]) * n_particles
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            for k, nm in enumerate(names):
+                if r[5 + k].strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl != "reference" else "gloo")
+    return world, rank, local
+
+
+def allreduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def oracle_cpu_rate(tg, mesh, p, state, n, budget_s=20.0, threads=0):
+    """FP64 oracle steps over the full state; returns (particle-steps/s, sample, cores)."""
+    import oracle
+    a = mesh.arrays()
+    om = oracle.Mesh(a["v3"], a["f3"], a["uv"], a["fuv"])
+    cen = a["v3"].mean(0)
+    st = dict(uv=state["uv"], theta=state["theta"], face=state["face"], r3d=state["r3d"],
+              ids=np.arange(n, dtype=np.int32))
+    cores = threads or os.cpu_count()
+    t0 = time.perf_counter()
+    oracle.model_step(om, p.oracle_dict(), st, 0, 0, centroid=cen, threads=cores)
+    t1 = time.perf_counter() - t0
+    steps = max(1, min(10, int(budget_s / max(t1, 1e-3))))
+    t0 = time.perf_counter()
+    for k in range(steps):
+        out = oracle.model_step(om, p.oracle_dict(), st, k + 1, 0, centroid=cen, threads=cores)
+        st = dict(uv=out["uv"], theta=out["theta"], face=out["face"], r3d=out["r3d"], ids=st["ids"])
+    dt = time.perf_counter() - t0
+    return n * steps / dt, "%d full steps of the %d-particle state (FP64 oracle, %d threads)" % (steps, n, cores), cores
+
+
+def seeded_state(mesh, n, seed):
+    """Area-weighted seeded placement in numpy (host only), for the CPU reference arm."""
+    a = mesh.arrays()
+    v3, f3, uv, fuv = a["v3"], a["f3"], a["uv"], a["fuv"]
+    rng = np.random.default_rng(seed)
+    A, B, C = v3[f3[:, 0]], v3[f3[:, 1]], v3[f3[:, 2]]
+    ar = 0.5 * np.linalg.norm(np.cross(B - A, C - A), axis=1)
+    cdf = np.cumsum(ar) / ar.sum()
+    f = np.minimum(np.searchsorted(cdf, rng.random(n)), len(cdf) - 1)
+    s, t = np.sqrt(rng.random(n)), rng.random(n)
+    w = np.stack([1 - s, s * (1 - t), s * t], 1)
+    p = w[:, 0, None] * uv[fuv[f, 0]] + w[:, 1, None] * uv[fuv[f, 1]] + w[:, 2, None] * uv[fuv[f, 2]]
+    r3 = w[:, 0, None] * A[f] + w[:, 1, None] * B[f] + w[:, 2, None] * C[f]
+    th = rng.random(n) * 2 * np.pi - np.pi
+    return dict(uv=p, theta=th, face=f.astype(np.int32), r3d=r3)
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    tg = importlib.import_module("2dtissue_gb300")
+    mesh, p, n = config2(tg)
+    state = seeded_state(mesh, n, 0)
+    import oracle
+    a = mesh.arrays()
+    om = oracle.Mesh(a["v3"], a["f3"], a["uv"], a["fuv"])
+    cen = a["v3"].mean(0)
+    cores = os.cpu_count()
+    st = dict(state, ids=np.arange(n, dtype=np.int32))
+    t0 = time.perf_counter()
+    for k in range(max(args.warmup, 1)):
+        out = oracle.model_step(om, p.oracle_dict(), st, k, 0, centroid=cen, threads=cores)
+        st = dict(uv=out["uv"], theta=out["theta"], face=out["face"], r3d=out["r3d"], ids=st["ids"])
+    t_full = (time.perf_counter() - t0) / max(args.warmup, 1)
+    # bounded sample: update a subset when the full K steps would exceed ~150 s
+    m = n if args.steps * t_full <= 150 else max(4096, int(n * 150 / (args.steps * t_full)))
+    sub = None if m == n else np.sort(np.random.default_rng(1).choice(n, m, replace=False)).astype(np.int32)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        out = oracle.model_step(om, p.oracle_dict(), st, args.warmup + k, 0, centroid=cen, subset=sub, threads=cores)
+        if sub is None:
+            st = dict(uv=out["uv"], theta=out["theta"], face=out["face"], r3d=out["r3d"], ids=st["ids"])
+    dt = time.perf_counter() - t0
+    value = m * args.steps / dt
+    sample = ("%d steps updating %s of the %d-particle state (FP64 oracle, %d threads)"
+              % (args.steps, "all" if sub is None else "%d" % m, n, cores))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded placement)",
+            "config": workload_config(mesh, p, n, "n/a (CPU)"),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+    world, rank, local = dist_setup(args)
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(local)
+    tg = importlib.import_module("2dtissue_gb300")
+    mesh, p, n = config2(tg)
+    sim = tg.Simulation(mesh, p, n, seed=rank, precision=32)
+    sim.start()
+    stream = torch.cuda.ExternalStream(sim.stream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def flush_l2(k):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 255)
+
+    for k in range(args.warmup):
+        flush_l2(k)
+        sim.step_async(1)
+    torch.cuda.synchronize()
+    assert sim.status() == 0, "device status set during warm-up"
+
+    # ---- timed region: K steps, each flushed + event-timed ----
+    sim.kernel_timing(True)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    clk = Clocks(local)
+    for k in range(args.steps):
+        flush_l2(k + 7)
+        ev[k][0].record(stream)
+        sim.step_async(1)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = clk.stop()
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    kt = sim.kernel_times()
+    sim.kernel_timing(False)
+    status = sim.status()
+    if status:
+        raise SystemExit("device status 0x%x in the timed region" % status)
+    total_ms = allreduce_max(total_ms, world)
+    value = world * n * args.steps / (total_ms * 1e-3)
+
+    # ---- dominant kernel roofline (k_step), from the events of the timed region ----
+    step_ms, step_n = kt["step"]
+    avg_s = step_ms * 1e-3 / max(step_n, 1)
+    alg = ALG_BYTES_PARTICLE * n + ALG_BYTES_FACE * mesh.F + ALG_BYTES_REPLICA
+    peak, peak_kind = measured_peak()
+    achieved = alg / avg_s / 1e9
+    traffic = profiled_traffic(n)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_source": peak_kind, "kernel": "k_step",
+                "kernel_ms": avg_s * 1e3, "algorithmic_bytes": alg}
+    step_frac = alg / (total_ms * 1e-3 / args.steps) / 1e9 / peak
+    shares = {k: v[0] / max(1e-12, sum(x[0] for x in kt.values())) for k, v in kt.items()}
+
+    # ---- steady state: graph-captured back-to-back steps, no flush (informational) ----
+    ga, gb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sim.step_async(16)
+    torch.cuda.synchronize()
+    ga.record(stream)
+    sim.step_async(128)
+    gb.record(stream)
+    torch.cuda.synchronize()
+    loop_rate = n * 128 / (ga.elapsed_time(gb) * 1e-3)
+
+    # ---- end to end through the C-ABI with pinned host buffers ----
+    def pinned(shape, dtype):
+        return torch.empty(shape, dtype=dtype, pin_memory=True).numpy()
+
+    hin = sim.get_state()
+    pin_in = dict(uv=pinned((n, 2), torch.float64), theta=pinned((n,), torch.float64),
+                  face=pinned((n,), torch.int32), r3d=pinned((n, 3), torch.float64))
+    for k in pin_in:
+        pin_in[k][...] = hin[k]
+    pin_out = dict(uv=pinned((n, 2), torch.float64), theta=pinned((n,), torch.float64),
+                   face=pinned((n,), torch.int32), r3d=pinned((n, 3), torch.float64),
+                   vel_uv=pinned((n, 2), torch.float64), nbr=pinned((n,), torch.int32))
+    e2e_steps = max(3, min(args.steps, 20))
+    sim.set_state(**pin_in)
+    sim.step(1)
+    sim.get_state(pin_out)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.set_state(**pin_in)
+        sim.step(1)
+        sim.get_state(pin_out)
+    e2e_s = allreduce_max(time.perf_counter() - t0, world)
+    e2e = {"value": world * n * e2e_steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(sum(v.nbytes for v in pin_in.values())),
+           "d2h_bytes_per_step": int(sum(v.nbytes for v in pin_out.values())),
+           "path": "tds_set_state (pinned H2D) + tds_step + tds_get_state (pinned D2H)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, sample, cores = oracle_cpu_rate(tg, mesh, p, sim.get_state(), n)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded placement)",
+                "config": workload_config(mesh, p, n, "flushed (256 MB write) before every timed step"),
+                "roofline": roofline, "step_hbm_frac": step_frac, "kernel_share": shares,
+                "graph_loop": {"value": loop_rate, "unit": UNIT, "note": "128 graph-captured steps, no flush"},
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": KERNELS_PER_STEP * args.steps, "clocks": clocks,
+                "parallelism": "replicas only (one independent 1M-particle system per GPU)"}
+        print(json.dumps(line), flush=True)
+    sim.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl != "reference":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,131 @@
+/*
+ * tds.h — C-ABI of 2dtissue_gb300: the per-step active-particle update of 2DTissue on a
+ * triangulated closed surface, run on one GB300 (sm_103a).
+ *
+ * The reference has no FFI; the boundary it sits behind is the C++ class _2DTissue
+ * (src/simulation/2DTissue.h:35-60) and the operator seam LocomotionHelperInterface
+ * (src/simulation/LocomotionHelperInterface.h:3-13). Each entry point below names the
+ * reference member it replaces. Conventions:
+ *   - every call returns an int status: TDS_OK (0) or a TDS_ERR_* code; no exception crosses
+ *     the boundary; tds_last_error() / tds_mesh_last_error() give the message;
+ *   - handles own their device memory; caller buffers are borrowed for the call only;
+ *   - one handle is used by one host thread at a time; handles are independent and each has
+ *     its own CUDA stream;
+ *   - particle arrays passed across the boundary are in particle-id order, structure of arrays.
+ */
+#ifndef TDS_H
+#define TDS_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TDS_OK 0
+#define TDS_ERR_ARG 1     /* invalid argument (reference: std::invalid_argument) */
+#define TDS_ERR_CUDA 2    /* CUDA runtime error, or no CUDA device */
+#define TDS_ERR_MESH 3    /* mesh could not be read / charted */
+#define TDS_ERR_STATE 4   /* the device status word is non-zero after a step (see TDS_STATUS_*) */
+#define TDS_ERR_NOMEM 5
+#define TDS_ERR_LIMIT 6   /* a size is above a stated maximum */
+
+/* Device status bits (reference: Validation::error_invalid_values -> exit(1),
+ * Validation::error_lost_particles -> throw, Validation.cpp:40-72). */
+#define TDS_STATUS_NONFINITE 1      /* NaN/Inf in a new position or polarity */
+#define TDS_STATUS_WRAP_LIMIT 2     /* more than 8 seam wraps in one step (position clamped) */
+#define TDS_STATUS_LOCATE_FALLBACK 4 /* no chart face contained the point (nearest face used) */
+#define TDS_STATUS_NBR_OVERFLOW 8   /* >= 1024 neighbours: fixed-point pair sums may overflow */
+#define TDS_STATUS_CELL_OVERFLOW 16 /* a cell-list rank overflowed its field */
+
+typedef struct tds_mesh tds_mesh;
+typedef struct tds_sim tds_sim;
+
+/* Model parameters (reference ctor arguments, 2DTissue.h:37-54: sigma -> radius,
+ * k -> k_rep, r_adh -> r_max, k_adh, v0, mu, step_size -> dt). */
+typedef struct tds_params {
+    double radius;  /* particle radius R; contact distance 2R */
+    double k_rep;   /* repulsion stiffness for d < 2R */
+    double k_adh;   /* adhesion stiffness for 2R <= d < r_max */
+    double r_max;   /* interaction cut-off (reference r_adh = 2.4 sigma) */
+    double v0;      /* self-propulsion speed */
+    double mu;      /* mobility */
+    double tau;     /* polarity relaxation time towards the velocity */
+    double align;   /* strength of alignment with the neighbours' polarity */
+    double eta;     /* angular noise amplitude: U[-eta/2, eta/2] per step */
+    double dt;      /* time step */
+    int force_mode; /* 0: v = v0 p + mu F_t;  1: reference speed-only |v| = v0 + |F_t| along p */
+    int reserved;
+} tds_params;
+
+/* Particle state in id order. Any pointer may be NULL where noted. */
+typedef struct tds_state_view {
+    double* uv;        /* 2N chart coordinates */
+    double* theta;     /* N polarity angle in the chart (radians) */
+    int* face;         /* N containing chart face (set: NULL or -1 entries -> located) */
+    double* r3d;       /* 3N 3D positions (set: NULL -> mapped from uv/face) */
+    double* vel_uv;    /* 2N chart velocity of the last step (get only, may be NULL) */
+    int* nbr_count;    /* N neighbours within r_max in the last step (get only, may be NULL) */
+} tds_state_view;
+
+/* ---- mesh + chart (reference: loadMeshFaces / SurfaceParametrization::create_uv_surface,
+ *      2DTissue.cpp:85-107; MeshCartographyLib is absent, this builds its own chart) ---- */
+int tds_mesh_ellipsoid(int level, double ax, double ay, double az, tds_mesh** out);
+int tds_mesh_bumpy_sphere(int level, double amp, double scale, tds_mesh** out);
+int tds_mesh_from_arrays(const double* v3, int V, const int* f3, int F, tds_mesh** out);
+int tds_mesh_load_off(const char* path, tds_mesh** out);
+int tds_mesh_save_off(const tds_mesh* m, const char* path);
+int tds_mesh_info(const tds_mesh* m, int* V, int* F, int* Vuv, double* area);
+/* v3: 3V, f3: 3F, uv: 2Vuv, fuv: 3F, uv2v: Vuv; any may be NULL */
+int tds_mesh_arrays(const tds_mesh* m, double* v3, int* f3, double* uv, int* fuv, int* uv2v);
+void tds_mesh_destroy(tds_mesh* m);
+const char* tds_mesh_last_error(void);
+
+/* ---- simulation (reference: _2DTissue ctor / start() / update() / is_finished() /
+ *      get_order_parameter(), 2DTissue.cpp:20-134,136-206,208-215) ---- */
+/* precision: 32 (FP32 state, the fast path) or 64 (FP64 build, the correctness path). */
+int tds_create(const tds_mesh* mesh, const tds_params* params, int n_particles, uint64_t seed, int precision,
+               tds_sim** out);
+/* Ragged ensemble of independent replicas in one set of launches; params has n_replicas entries. */
+int tds_ensemble_create(const tds_mesh* mesh, int n_replicas, const int* n_particles, const tds_params* params,
+                        uint64_t seed, int precision, tds_sim** out);
+/* Area-weighted random placement, polarity uniform in the face tangent frame (Philox, seeded). */
+int tds_start(tds_sim* sim);
+/* n_steps of the update. noise: NULL (Philox noise) or n_steps x N angle increments in id order. */
+int tds_step(tds_sim* sim, int n_steps, const double* noise);
+/* update() semantics: one step, then the state is copied into `out` (host buffers). */
+int tds_update(tds_sim* sim, tds_state_view* out);
+int tds_set_state(tds_sim* sim, const tds_state_view* in);
+int tds_get_state(tds_sim* sim, tds_state_view* out);
+/* phi = |sum normalize((r - c) x v)| / N, psi = |sum v/|v|| / N per step and replica:
+ * arrays of cap entries, step-major ([step][replica]); *n_steps gets the number of steps stored. */
+int tds_get_order_parameter(tds_sim* sim, double* phi, double* psi, int cap, int* n_steps);
+int tds_get_step(const tds_sim* sim, int64_t* step);
+int tds_get_status(tds_sim* sim, int* status);
+int tds_clear_status(tds_sim* sim);
+int tds_num_particles(const tds_sim* sim, int* n_total, int* n_replicas);
+/* Launches n_steps on the handle's stream and returns without waiting; the status word is
+ * checked by the next tds_step / tds_get_status. For pipelined callers and device-timed loops. */
+int tds_step_async(tds_sim* sim, int n_steps);
+/* Per-kernel CUDA-event timing of directly launched steps (graphs are not used while enabled).
+ * tds_kernel_times returns, per kernel (0 scan, 1 scatter, 2 step, 3 finalize), the summed
+ * device time in ms and the launch count since timing was enabled. */
+int tds_kernel_timing(tds_sim* sim, int enable);
+int tds_kernel_times(tds_sim* sim, double* total_ms, long long* launches);
+/* The CUDA stream every kernel of this handle runs on (cudaStream_t). */
+int tds_stream(tds_sim* sim, void** stream);
+/* Kernels launched per step (for launch accounting). */
+int tds_kernels_per_step(const tds_sim* sim, int* n);
+const char* tds_last_error(const tds_sim* sim);
+void tds_destroy(tds_sim* sim);
+
+/* ---- test hooks ---- */
+/* Runs the device seam wrap (the model form of EuclideanTiling::diagonal_seam_edges_square_border,
+ * EuclideanTiling.cpp:31-69) on n points: uv holds the advanced points on entry and the wrapped
+ * points on return; theta and vel_uv (2n, may be NULL) are rotated with them. */
+int tds_debug_seam_wrap(int n, const double* uv_old, double* uv, double* theta, double* vel_uv, int* n_wraps,
+                        int precision);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TDS_H */

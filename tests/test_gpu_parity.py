@@ -1,0 +1,274 @@
+"""Per-step parity of the CUDA path with the FP64 oracle, through the C-ABI.
+
+Every comparison starts both sides from the identical state (the GPU state read back; the oracle
+gets exactly those values) with identical Philox noise. Tolerances (from the contract):
+  * neighbour counts and face indices bit-exact, except particles with a pair within 1e-6 of the
+    cut-off (neighbours) or a new position within 1e-6 of a face edge (faces);
+  * positions and polarity: 1e-5 relative in FP32, 1e-12 in the FP64 build (atol for values near 0).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+from scipy.spatial import cKDTree
+
+from conftest import get_mesh, oracle_mesh
+
+pytestmark = pytest.mark.gpu
+
+TOL = {32: dict(rtol=1e-5, atol=1e-6), 64: dict(rtol=1e-12, atol=1e-13)}
+BAND = 1e-6
+
+
+def cutoff_band(r3d, r_max, eps=BAND):
+    """Particles with some pair distance within eps of r_max (ambiguous neighbour membership)."""
+    tree = cKDTree(r3d)
+    pairs = tree.query_pairs(r_max + 10 * eps, output_type="ndarray")
+    if len(pairs) == 0:
+        return np.zeros(len(r3d), bool)
+    d = np.linalg.norm(r3d[pairs[:, 0]] - r3d[pairs[:, 1]], axis=1)
+    amb = pairs[np.abs(d - r_max) < eps * max(1.0, np.abs(r3d).max())]
+    out = np.zeros(len(r3d), bool)
+    out[amb.ravel()] = True
+    return out
+
+
+def compare_step(orc, om, params, g0, g1, step, seed, precision, subset=None, ids=None, local_bits=31,
+                 centroid=(0, 0, 0)):
+    """g0: GPU state before the step (id order), g1: after. Returns the oracle output."""
+    n = len(g0["theta"])
+    st = dict(uv=g0["uv"], theta=g0["theta"], face=g0["face"], r3d=g0["r3d"],
+              ids=np.arange(n, dtype=np.int32) if ids is None else ids)
+    out = orc.model_step(om, params, st, step, seed, local_bits=local_bits, centroid=centroid, subset=subset)
+    sel = np.arange(n) if subset is None else np.asarray(subset)
+    amb = cutoff_band(g0["r3d"], params["r_max"])[sel]
+    tol = TOL[precision]
+    ok = ~amb
+    # neighbour counts: exact outside the band
+    np.testing.assert_array_equal(g1["nbr"][sel][ok], out["nbr"][ok])
+    # faces: exact unless the point sits on a shared edge / vertex
+    fmis = np.where(g1["face"][sel] != out["face"])[0]
+    for k in fmis:
+        i = sel[k]
+        f, mode = om.locate(*g1["uv"][i], int(g1["face"][i]))
+        assert f == g1["face"][i] or mode != 0, "face mismatch away from an edge for particle %d" % i
+    assert len(fmis) <= max(2, 1e-3 * len(sel))
+    good = ok.copy()
+    good[fmis] = False
+    np.testing.assert_allclose(g1["uv"][sel][good], out["uv"][good], **tol)
+    np.testing.assert_allclose(g1["r3d"][sel][good], out["r3d"][good],
+                               rtol=tol["rtol"], atol=tol["atol"] * max(1.0, np.abs(out["r3d"]).max()))
+    np.testing.assert_allclose(np.cos(g1["theta"][sel][good]), np.cos(out["theta"][good]), **tol)
+    np.testing.assert_allclose(np.sin(g1["theta"][sel][good]), np.sin(out["theta"][good]), **tol)
+    np.testing.assert_allclose(g1["vel_uv"][sel][good], out["vel_uv"][good],
+                               rtol=tol["rtol"] * 10, atol=tol["atol"] * 10)
+    return out
+
+
+@pytest.fixture(scope="module")
+def cfg1(tg, orc, mesh_l4):
+    om, arr = oracle_mesh(orc, mesh_l4)
+    return om, arr["v3"].mean(0)
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_config1_per_step_parity(tg, orc, mesh_l4, cfg1, precision):
+    """Config 1: (2,1,1) ellipsoid L4, 100 particles, 50 steps; each step checked."""
+    om, cen = cfg1
+    p = tg.Params()
+    sim = tg.Simulation(mesh_l4, p, 100, seed=0, precision=precision)
+    sim.start()
+    g0 = sim.get_state()
+    phis = []
+    for t in range(50):
+        sim.step(1)
+        g1 = sim.get_state()
+        out = compare_step(orc, om, p.oracle_dict(), g0, g1, t, 0, precision, centroid=cen)
+        phis.append(np.linalg.norm(out["phi_sums"][:3]) / 100)
+        g0 = g1
+    phi, psi = sim.order_parameter()
+    np.testing.assert_allclose(phi[:, 0], phis, rtol=1e-5 if precision == 32 else 1e-10, atol=1e-6)
+    assert sim.status() == 0
+
+
+def test_config1_denser_parity(tg, orc, mesh_l4, cfg1):
+    """2000 particles on the config-1 mesh (many neighbours, wraps, face changes), FP64 and FP32."""
+    om, cen = cfg1
+    p = tg.Params()
+    for precision in (64, 32):
+        sim = tg.Simulation(mesh_l4, p, 2000, seed=5, precision=precision)
+        sim.start()
+        sim.step(3)
+        g0 = sim.get_state()
+        sim.step(1)
+        g1 = sim.get_state()
+        out = compare_step(orc, om, p.oracle_dict(), g0, g1, 3, 5, precision, centroid=cen)
+        assert out["nbr"].mean() > 1.0
+
+
+def test_reference_seam_wrap_kat_on_device(tg):
+    kat = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_kats.json")))["seam_wrap"]
+    uo = np.array(kat["uv_old"]).reshape(-1, 2)
+    u = np.array(kat["uv"]).reshape(-1, 2)
+    for precision in (64, 32):
+        out, th, v, nw = tg.debug_seam_wrap(uo, u, np.deg2rad(kat["n"]), np.ones((3, 2)), precision=precision)
+        np.testing.assert_allclose(out.ravel(), kat["expected"], atol=kat["tol"] if precision == 64 else 1e-6)
+        exp_th = np.deg2rad(np.array(kat["n"]) + np.array([-360, -180, -90]))  # reference rotations
+        np.testing.assert_allclose(np.cos(th), np.cos(exp_th), atol=1e-6)
+        np.testing.assert_allclose(np.sin(th), np.sin(exp_th), atol=1e-6)
+        assert list(nw) == [2, 2, 1]
+
+
+def test_seam_wrap_random_vs_oracle(tg, orc):
+    rng = np.random.default_rng(7)
+    n = 4000
+    s = rng.random((n, 2))
+    e = s + rng.normal(size=(n, 2)) * 0.7
+    th = rng.random(n) * 6 - 3
+    v = rng.normal(size=(n, 2))
+    gu, gth, gv, gnw = tg.debug_seam_wrap(s, e, th, v, precision=64)
+    for i in range(n):
+        oe, oth, ov, onw, rc = orc.model_wrap(s[i], e[i], th[i], v[i])
+        np.testing.assert_allclose(gu[i], oe, atol=1e-12)
+        np.testing.assert_allclose(gv[i], ov, atol=1e-12)
+        assert abs(gth[i] - oth) < 1e-12 and gnw[i] == onw
+
+
+def config2_params(tg, mesh):
+    N = 1 << 20
+    R = float(np.sqrt(0.5 * mesh.area / (np.pi * N)))
+    return N, tg.Params(radius=R, r_max=2.4 * R, eta=0.3, dt=0.01)
+
+
+def test_config2_subset_parity(tg, orc):
+    """Config 2: (20,10,10) ellipsoid L7, 1,048,576 particles, FP32; the oracle gets the full state
+    and updates a seeded subset of 4096 particles."""
+    mesh = get_mesh(tg, 7, (20.0, 10.0, 10.0))
+    N, p = config2_params(tg, mesh)
+    om, arr = oracle_mesh(orc, mesh)
+    sim = tg.Simulation(mesh, p, N, seed=2, precision=32)
+    sim.start()
+    sim.step(4)
+    g0 = sim.get_state()
+    sim.step(1)
+    g1 = sim.get_state()
+    sub = np.sort(np.random.default_rng(0).choice(N, 4096, replace=False)).astype(np.int32)
+    out = compare_step(orc, om, p.oracle_dict(), g0, g1, 4, 2, 32, subset=sub, centroid=arr["v3"].mean(0))
+    assert 1.0 < out["nbr"].mean() < 8.0
+
+
+def test_ensemble_parity(tg, orc, mesh_l4, cfg1):
+    """Ragged ensemble: each replica matches the oracle run with that replica's parameters."""
+    om, cen = cfg1
+    ns = [64, 200, 1000, 37, 513]
+    ps = [tg.Params(eta=e, v0=v) for e, v in zip([0.1, 2.0, 0.5, 6.0, 0.0], [0.5, 1.5, 1.0, 0.7, 1.2])]
+    sim = tg.Simulation(mesh_l4, ps, ns, seed=4, precision=32)
+    sim.start()
+    sim.step(2)
+    g0 = sim.get_state()
+    sim.step(1)
+    g1 = sim.get_state()
+    lb = int(np.ceil(np.log2(max(ns))))
+    off = np.concatenate([[0], np.cumsum(ns)])
+    phi, psi = sim.order_parameter()
+    for r, n in enumerate(ns):
+        sl = slice(off[r], off[r + 1])
+        a = {k: v[sl] for k, v in g0.items()}
+        b = {k: v[sl] for k, v in g1.items()}
+        ids = ((r << lb) | np.arange(n)).astype(np.int32)
+        out = compare_step(orc, om, ps[r].oracle_dict(), a, b, 2, 4, 32, ids=ids, local_bits=lb, centroid=cen)
+        np.testing.assert_allclose(phi[2, r], np.linalg.norm(out["phi_sums"][:3]) / n, rtol=1e-4, atol=1e-6)
+        np.testing.assert_allclose(psi[2, r], np.linalg.norm(out["phi_sums"][3:]) / n, rtol=1e-4, atol=1e-6)
+
+
+def test_deterministic_replay(tg, mesh_l4):
+    """Order-independent (fixed-point) pair sums: two runs are bitwise identical."""
+    outs = []
+    for _ in range(2):
+        sim = tg.Simulation(mesh_l4, tg.Params(), 3000, seed=9, precision=32)
+        sim.start()
+        sim.step(40)
+        outs.append(sim.get_state())
+    for k in outs[0]:
+        np.testing.assert_array_equal(outs[0][k], outs[1][k])
+
+
+def test_injected_noise_matches_philox(tg, mesh_l4, orc):
+    p = tg.Params()
+    a = tg.Simulation(mesh_l4, p, 300, seed=3, precision=64)
+    a.start()
+    s0 = a.get_state()
+    xi = np.zeros((2, 300))
+    for t in range(2):
+        for i in range(300):
+            w = orc.philox4x32_10([t, 0, i, 0], [3, 0])[0]
+            xi[t, i] = p.eta * ((w >> 8) / 16777216.0 - 0.5)
+    a.step(2)
+    b = tg.Simulation(mesh_l4, p, 300, seed=3, precision=64)
+    b.set_state(s0["uv"], s0["theta"], s0["face"], s0["r3d"])
+    b.step(2, noise=xi)
+    sa, sb = a.get_state(), b.get_state()
+    np.testing.assert_allclose(sa["uv"], sb["uv"], rtol=0, atol=1e-13)
+
+
+def test_graph_and_direct_launches_agree(tg, mesh_l4):
+    a = tg.Simulation(mesh_l4, tg.Params(), 500, seed=1)
+    a.start()
+    a.step(37)  # 2 graph chunks + 5 direct
+    b = tg.Simulation(mesh_l4, tg.Params(), 500, seed=1)
+    b.start()
+    for _ in range(37):
+        b.step(1)
+    sa, sb = a.get_state(), b.get_state()
+    for k in sa:
+        np.testing.assert_array_equal(sa[k], sb[k])
+
+
+def test_nonfinite_state_reports_status(tg, mesh_l4):
+    sim = tg.Simulation(mesh_l4, tg.Params(), 200, seed=1)
+    sim.start()
+    s = sim.get_state()
+    s["theta"][17] = np.nan
+    sim.set_state(s["uv"], s["theta"], s["face"], s["r3d"])
+    with pytest.raises(tg.TdsError) as e:
+        sim.step(1)
+    assert e.value.code == 4
+    assert sim.status() & 1
+    sim.clear_status()
+    assert sim.status() == 0
+
+
+def test_start_places_particles_on_the_surface(tg, orc, mesh_l4, cfg1):
+    om, _ = cfg1
+    sim = tg.Simulation(mesh_l4, tg.Params(), 5000, seed=12, precision=64)
+    sim.start()
+    s = sim.get_state()
+    for i in range(0, 5000, 97):
+        np.testing.assert_allclose(om.map(s["face"][i], *s["uv"][i]), s["r3d"][i], atol=1e-12)
+    # area-weighted placement: mean particles per unit area is uniform over the two halves x<0, x>0
+    assert abs((s["r3d"][:, 0] < 0).mean() - 0.5) < 0.03
+
+
+def test_long_run_polar_order_statistics(tg, orc, mesh_l4, cfg1):
+    """Long-run polar order over 32 seeds: GPU FP32 and oracle FP64 means agree within 2 SE."""
+    om, cen = cfg1
+    p = tg.Params()
+    g, o = [], []
+    for seed in range(32):
+        sim = tg.Simulation(mesh_l4, p, 100, seed=seed)
+        sim.start()
+        st = sim.get_state()
+        sim.step(50)
+        phi, _ = sim.order_parameter()
+        g.append(phi[-10:, 0].mean())
+        s = dict(uv=st["uv"], theta=st["theta"], face=st["face"], r3d=st["r3d"], ids=np.arange(100, dtype=np.int32))
+        vals = []
+        for t in range(50):
+            out = orc.model_step(om, p.oracle_dict(), s, t, seed, centroid=cen)
+            s = dict(uv=out["uv"], theta=out["theta"], face=out["face"], r3d=out["r3d"], ids=s["ids"])
+            vals.append(np.linalg.norm(out["phi_sums"][:3]) / 100)
+        o.append(np.mean(vals[-10:]))
+    g, o = np.array(g), np.array(o)
+    se = np.sqrt(g.var(ddof=1) / len(g) + o.var(ddof=1) / len(o))
+    assert abs(g.mean() - o.mean()) < 2 * se + 1e-9
