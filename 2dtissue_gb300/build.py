@@ -13,6 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "lib2dtissue_gb300.so")
+CLI = os.path.join(OUT, "tds_cli")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
@@ -65,6 +66,10 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         tmp = LIB + ".tmp%d" % os.getpid()
         _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs)
         os.replace(tmp, LIB)
+    cli_src = os.path.join(CSRC, "cli.cpp")
+    if force or _stale(CLI, [cli_src, LIB, os.path.join(CSRC, "tissue.hpp")]):
+        _run(["g++", "-O2", "-std=c++17", cli_src, "-o", CLI, "-L" + OUT, "-l2dtissue_gb300",
+              "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

@@ -1,0 +1,144 @@
+// C++ facade over the C-ABI with the reference's interface: class _2DTissue
+// (src/simulation/2DTissue.h:35-60) and its Particle / System records (src/simulation/Struct.h:9-29).
+// Header-only; link against lib2dtissue_gb300.so.
+//
+// Differences from the reference, by design:
+//   * step_size is the time step; the reference CLI passes --step-time into the v0 slot
+//     (main.cpp:76-84) -- the CLI here maps --step-time to step_size explicitly;
+//   * errors throw std::runtime_error carrying the C-ABI message (the reference exits or throws
+//     from Validation, Validation.cpp:40-72);
+//   * Kafka/SQLite sinks and the particle "Innenleben" are not part of this path.
+#pragma once
+#include <cmath>
+#include <cstdio>
+#include <filesystem>
+#include <fstream>
+#include <iomanip>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/tds.h"
+
+namespace tds {
+
+struct Particle {
+    double x_UV, y_UV;
+    double x_velocity_UV, y_velocity_UV;
+    double alignment_UV;  // polarity angle in the chart, degrees (the reference stores int degrees)
+    double compass_north_pole_UV = 0, compass_south_pole_UV = 0;  // never set by the reference either
+    double x_3D, y_3D, z_3D;
+    int neighbor_count;
+};
+
+struct System {
+    double order_parameter;
+    std::vector<Particle> particles;
+};
+
+class Tissue2D {
+  public:
+    Tissue2D(bool save_data, bool particle_innenleben, bool free_boundary, std::string mesh_path, int particle_count,
+             int step_count = 1, double v0 = 0.1, bool use_kafka = false, double k = 1, double k_next = 10,
+             double v0_next = 0.1, double sigma = 0.4166666666666667, double mu = 1, double r_adh = 1,
+             double k_adh = 0.75, double step_size = 0.001, int map_cache_count = 30, double tau = 1.0,
+             double align = 0.5, double eta = 0.0, uint64_t seed = 0, int precision = 32)
+        : save_data_(save_data), n_(particle_count), step_count_(step_count) {
+        (void)particle_innenleben, (void)free_boundary, (void)use_kafka, (void)k_next, (void)v0_next;
+        (void)map_cache_count;
+        int rc = mesh_path.empty() ? tds_mesh_ellipsoid(4, 2.0, 1.0, 1.0, &mesh_)
+                                   : tds_mesh_load_off(mesh_path.c_str(), &mesh_);
+        if (rc) throw std::runtime_error(std::string("mesh: ") + tds_mesh_last_error());
+        tds_params p{};
+        p.radius = sigma;
+        p.k_rep = k;
+        p.k_adh = k_adh;
+        p.r_max = r_adh;
+        p.v0 = v0;
+        p.mu = mu;
+        p.tau = tau;
+        p.align = align;
+        p.eta = eta;
+        p.dt = step_size;
+        p.force_mode = 0;
+        rc = tds_create(mesh_, &p, particle_count, seed, precision, &sim_);
+        if (rc) {
+            tds_mesh_destroy(mesh_);
+            throw std::runtime_error("tds_create failed (code " + std::to_string(rc) + ")");
+        }
+        uv_.resize(2 * (size_t)n_), th_.resize(n_), r3_.resize(3 * (size_t)n_), vel_.resize(2 * (size_t)n_);
+        face_.resize(n_), cnt_.resize(n_);
+    }
+    Tissue2D(const Tissue2D&) = delete;
+    Tissue2D& operator=(const Tissue2D&) = delete;
+    ~Tissue2D() {
+        tds_destroy(sim_);
+        tds_mesh_destroy(mesh_);
+    }
+
+    void start() { check(tds_start(sim_)); }
+
+    System update() {
+        tds_state_view v{uv_.data(), th_.data(), face_.data(), r3_.data(), vel_.data(), cnt_.data()};
+        check(tds_update(sim_, &v));
+        ++current_step_;
+        System sys;
+        int ns = 0;
+        std::vector<double> phi(current_step_);
+        check(tds_get_order_parameter(sim_, phi.data(), nullptr, (int)phi.size(), &ns));
+        sys.order_parameter = ns > 0 ? phi[ns - 1] : 0.0;
+        sys.particles.resize(n_);
+        for (int i = 0; i < n_; ++i) {
+            Particle& q = sys.particles[i];
+            q.x_UV = uv_[2 * i], q.y_UV = uv_[2 * i + 1];
+            q.x_velocity_UV = vel_[2 * i], q.y_velocity_UV = vel_[2 * i + 1];
+            q.alignment_UV = th_[i] * 180.0 / M_PI;
+            q.x_3D = r3_[3 * i], q.y_3D = r3_[3 * i + 1], q.z_3D = r3_[3 * i + 2];
+            q.neighbor_count = cnt_[i];
+        }
+        if (save_data_) save_our_data();
+        return sys;
+    }
+
+    bool is_finished() const { return current_step_ >= step_count_; }
+
+    std::vector<double> get_order_parameter() {
+        std::vector<double> phi(step_count_, 0.0);
+        int ns = 0;
+        check(tds_get_order_parameter(sim_, phi.data(), nullptr, step_count_, &ns));
+        return phi;
+    }
+
+    tds_sim* handle() { return sim_; }
+
+  private:
+    void check(int rc) {
+        if (rc) throw std::runtime_error(std::string("tds: ") + tds_last_error(sim_));
+    }
+    // CSV layout of save_matrix_to_csv (IO.h:40-69): 15 significant digits, one row per particle,
+    // files r_data_<step>.csv, r_data_3D_<step>.csv, particles_color_<step>.csv in ./data.
+    void save_our_data() {
+        std::filesystem::create_directories("data");
+        write_csv("data/r_data_" + std::to_string(current_step_) + ".csv", uv_.data(), 2);
+        write_csv("data/r_data_3D_" + std::to_string(current_step_) + ".csv", r3_.data(), 3);
+        std::ofstream f("data/particles_color_" + std::to_string(current_step_) + ".csv");
+        for (int i = 0; i < n_; ++i) f << cnt_[i] << "\n";
+    }
+    void write_csv(const std::string& path, const double* a, int cols) {
+        std::ofstream f(path);
+        f << std::setprecision(15);
+        for (int i = 0; i < n_; ++i) {
+            for (int c = 0; c < cols; ++c) f << (c ? "," : "") << a[(size_t)i * cols + c];
+            f << "\n";
+        }
+    }
+
+    bool save_data_;
+    int n_, step_count_, current_step_ = 0;
+    tds_mesh* mesh_ = nullptr;
+    tds_sim* sim_ = nullptr;
+    std::vector<double> uv_, th_, r3_, vel_;
+    std::vector<int> face_, cnt_;
+};
+
+}  // namespace tds

@@ -325,6 +325,20 @@ def run_gpu(args):
     sim.close()
 
 
+def run_profile(args):
+    """Minimal driver for ncu: the config-2 system, `warmup` steps, then `steps` steps; no timing."""
+    import torch
+    tg = importlib.import_module("2dtissue_gb300")
+    mesh, p, n = config2(tg)
+    sim = tg.Simulation(mesh, p, n, seed=0, precision=32)
+    sim.start()
+    sim.step(args.warmup)
+    sim.step_async(args.steps)
+    torch.cuda.synchronize()
+    assert sim.status() == 0
+    sim.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -332,7 +346,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--profile", action="store_true", help="only run warmup + steps (for ncu)")
     args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":
