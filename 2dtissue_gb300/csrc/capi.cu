@@ -56,7 +56,11 @@ struct tds_sim {
     int R = 1, N = 0, local_bits = 31;
     std::vector<int> n_rep, off;
     std::vector<tds_params> prm;
-    std::vector<tds::Fold> fold;
+    std::vector<int> level_of;  // replica -> cell level
+    int2* rows = nullptr;       // all levels' row tables
+    int4* ivals = nullptr;      // all levels' x-intervals
+    int4* adj = nullptr;        // chart edge adjacency per face
+    int* tile_sum = nullptr;    // [2][n_tiles] per-tile counts (step parity)
     uint64_t seed = 0;
     long long step = 0;  // completed steps
     const tds_mesh* mesh = nullptr;
@@ -72,8 +76,8 @@ struct tds_sim {
     long long M = 0;
     int n_tiles = 0;
     void* pos[2] = {nullptr, nullptr};
+    void* pol[2] = {nullptr, nullptr};
     void* uv[2] = {nullptr, nullptr};
-    int* face[2] = {nullptr, nullptr};
     int* ids[2] = {nullptr, nullptr};
     void* vel[2] = {nullptr, nullptr};
     int* cnt[2] = {nullptr, nullptr};
@@ -82,8 +86,6 @@ struct tds_sim {
     int* perm = nullptr;
     int* start = nullptr;
     int* count = nullptr;
-    unsigned long long* tile_state = nullptr;
-    unsigned* tickets = nullptr;
     unsigned long long* phi_acc = nullptr;
     double* series = nullptr;
     long long series_cap = 0;  // steps
@@ -151,18 +153,71 @@ int upload_tables(tds_sim* s) {
     CK(cudaMemcpy(s->bin_start, t.bin_start.data(), t.bin_start.size() * sizeof(int), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(s->bin_faces, t.bin_faces.data(), t.bin_faces.size() * sizeof(int), cudaMemcpyHostToDevice));
 
-    // replica table: parameters, fixed-point scales and cell-grid folds
+    // chart edge adjacency (int4 per face: the three edge neighbours, -1 on the border)
+    {
+        std::vector<int> adj;
+        tds::build_face_adjacency(s->mesh->m, adj);
+        std::vector<int4> a4(t.F);
+        for (int f = 0; f < t.F; ++f) a4[f] = make_int4(adj[3 * f], adj[3 * f + 1], adj[3 * f + 2], -1);
+        if ((rc = dalloc(s, &s->adj, a4.size() * sizeof(int4)))) return rc;
+        CK(cudaMemcpy(s->adj, a4.data(), a4.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    }
+
+    // cell levels: cell size r_max * 2^k; a replica takes the finest level whose surface-cell
+    // count is at most max(64, 4 N_r), so that small replicas do not scan many empty cells
+    struct Level {
+        double rmax;
+        int k;
+        double origin[3];
+        tds::CellLevel L;
+    };
+    std::vector<Level> levels;
+    auto get_level = [&](double rmax, int k) -> int {
+        for (size_t i = 0; i < levels.size(); ++i)
+            if (levels[i].rmax == rmax && levels[i].k == k) return (int)i;
+        Level lv;
+        lv.rmax = rmax, lv.k = k;
+        const double h = std::ldexp(rmax, k);
+        for (int d = 0; d < 3; ++d) lv.origin[d] = t.lo[d] - 2.0 * h;
+        tds::build_cell_level(s->mesh->m, h, lv.origin, lv.L);
+        levels.push_back(std::move(lv));
+        return (int)levels.size() - 1;
+    };
+    s->level_of.assign(s->R, 0);
+    for (int r = 0; r < s->R; ++r) {
+        int li = 0;
+        for (int k = 0; k <= 6; ++k) {
+            li = get_level(s->prm[r].r_max, k);
+            if (levels[li].L.C <= std::max(64, 4 * s->n_rep[r])) break;
+        }
+        s->level_of[r] = li;
+    }
+    std::vector<int> row_off(levels.size());
+    std::vector<int2> rows;
+    std::vector<int4> ivals;
+    for (size_t i = 0; i < levels.size(); ++i) {
+        const tds::CellLevel& L = levels[i].L;
+        row_off[i] = (int)rows.size();
+        const int ib = (int)ivals.size();
+        for (size_t r = 0; r < L.rows.size() / 2; ++r) rows.push_back(make_int2(L.rows[2 * r] + ib, L.rows[2 * r + 1]));
+        for (size_t v = 0; v < L.ivals.size() / 4; ++v)
+            ivals.push_back(make_int4(L.ivals[4 * v], L.ivals[4 * v + 1], L.ivals[4 * v + 2], 0));
+    }
+    if (ivals.empty()) ivals.push_back(make_int4(0, -1, 0, 0));
+    if ((rc = dalloc(s, &s->rows, rows.size() * sizeof(int2)))) return rc;
+    if ((rc = dalloc(s, &s->ivals, ivals.size() * sizeof(int4)))) return rc;
+    CK(cudaMemcpy(s->rows, rows.data(), rows.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->ivals, ivals.data(), ivals.size() * sizeof(int4), cudaMemcpyHostToDevice));
+
+    // replica table: parameters, fixed-point scales, cell level and bucket range
     std::vector<RepParams<real>> rp(s->R);
     long long base = 0;
-    double hmax = 0;
-    for (int r = 0; r < s->R; ++r) hmax = std::max(hmax, s->prm[r].r_max);
-    for (int k = 0; k < 3; ++k) s->origin[k] = t.lo[k] - 2.0 * hmax;
-    s->fold.resize(s->R);
     for (int r = 0; r < s->R; ++r) {
         const tds_params& p = s->prm[r];
         RepParams<real>& q = rp[r];
         std::memset(&q, 0, sizeof q);
-        const double h = p.r_max;
+        const Level& lv = levels[s->level_of[r]];
+        const double h = lv.L.h;
         q.twoR = (real)(2 * p.radius);
         q.inv_twoR = (real)(1.0 / (2 * p.radius));
         q.k = (real)p.k_rep;
@@ -183,13 +238,14 @@ int upload_tables(tds_sim* s) {
         q.phiscale = std::ldexp(1.0, 62 - ceil_log2((long long)s->n_rep[r] + 1));
         q.inv_n = 1.0 / std::max(1, s->n_rep[r]);
         q.force_mode = p.force_mode;
-        tds::Fold fo = tds::choose_fold(s->n_rep[r], t, h);
-        s->fold[r] = fo;
+        q.ox = (real)lv.origin[0], q.oy = (real)lv.origin[1], q.oz = (real)lv.origin[2];
         q.base = (int)base;
-        q.lx = fo.lx, q.ly = fo.ly, q.lz = fo.lz;
+        q.C = lv.L.C;
+        q.gx = lv.L.gx, q.gy = lv.L.gy, q.gz = lv.L.gz;
+        q.row_off = row_off[s->level_of[r]];
         q.n = s->n_rep[r];
         q.off = s->off[r];
-        base += fo.M;
+        base += (long long)lv.L.C + 1;  // + the bucket of particles off the surface cells
     }
     if (base > (1ll << 30)) return fail(s, TDS_ERR_LIMIT, "cell-list buckets exceed 2^30");
     s->M = base;
@@ -204,8 +260,8 @@ int alloc_state(tds_sim* s) {
     int rc;
     for (int b = 0; b < 2; ++b) {
         if ((rc = dalloc(s, (R4<real>**)&s->pos[b], N * sizeof(R4<real>)))) return rc;
+        if ((rc = dalloc(s, (R4<real>**)&s->pol[b], N * sizeof(R4<real>)))) return rc;
         if ((rc = dalloc(s, (R2<real>**)&s->uv[b], N * sizeof(R2<real>)))) return rc;
-        if ((rc = dalloc(s, &s->face[b], N * sizeof(int)))) return rc;
         if ((rc = dalloc(s, &s->ids[b], N * sizeof(int)))) return rc;
         if ((rc = dalloc(s, (R2<real>**)&s->vel[b], N * sizeof(R2<real>)))) return rc;
         if ((rc = dalloc(s, &s->cnt[b], N * sizeof(int)))) return rc;
@@ -216,8 +272,7 @@ int alloc_state(tds_sim* s) {
     if ((rc = dalloc(s, &s->start, (size_t)(s->M + 1) * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->count, (size_t)s->M * sizeof(int)))) return rc;
     s->n_tiles = (int)((s->M + tdsk::kScanTile - 1) / tdsk::kScanTile);
-    if ((rc = dalloc(s, &s->tile_state, (size_t)s->n_tiles * sizeof(unsigned long long)))) return rc;
-    if ((rc = dalloc(s, &s->tickets, 2 * sizeof(unsigned)))) return rc;
+    if ((rc = dalloc(s, &s->tile_sum, (size_t)2 * s->n_tiles * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->phi_acc, (size_t)s->R * tdsk::kPhiCopies * 6 * sizeof(unsigned long long)))) return rc;
     if ((rc = dalloc(s, &s->status, sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->d_step, sizeof(long long)))) return rc;
@@ -225,8 +280,7 @@ int alloc_state(tds_sim* s) {
     if ((rc = dalloc(s, &s->st_d, 8 * N * sizeof(double)))) return rc;
     if ((rc = dalloc(s, &s->st_i, 2 * N * sizeof(int)))) return rc;
     CK(cudaMemset(s->count, 0, (size_t)s->M * sizeof(int)));
-    CK(cudaMemset(s->tile_state, 0, (size_t)s->n_tiles * sizeof(unsigned long long)));
-    CK(cudaMemset(s->tickets, 0, 2 * sizeof(unsigned)));
+    CK(cudaMemset(s->tile_sum, 0, (size_t)2 * s->n_tiles * sizeof(int)));
     CK(cudaMemset(s->phi_acc, 0, (size_t)s->R * tdsk::kPhiCopies * 6 * sizeof(unsigned long long)));
     CK(cudaMemset(s->status, 0, sizeof(int)));
     const int nN = s->N;
@@ -311,8 +365,8 @@ void launch_one_step(tds_sim* s, const real* noise) {
     cudaStream_t st = s->stream;
     {
         KernelTimer kt(s, 0);
-        tdsk::k_scan<<<s->n_tiles, tdsk::kScanThreads, 0, st>>>(s->count, s->start, s->M, s->tile_state,
-                                                                 s->tickets, s->d_step, s->status);
+        tdsk::k_scan<<<s->n_tiles, tdsk::kScanThreads, 0, st>>>(s->count, s->start, s->M, s->tile_sum, s->n_tiles,
+                                                                 s->d_step);
     }
     const int nb = (s->N + 255) / 256;
     {
@@ -321,12 +375,12 @@ void launch_one_step(tds_sim* s, const real* noise) {
     }
     tdsk::StepArgs<real> a;
     a.pos = (const R4<real>*)s->pos[c];
+    a.pol = (const R4<real>*)s->pol[c];
     a.uv = (const R2<real>*)s->uv[c];
-    a.face = s->face[c];
     a.ids = s->ids[c];
     a.pos_o = (R4<real>*)s->pos[o];
+    a.pol_o = (R4<real>*)s->pol[o];
     a.uv_o = (R2<real>*)s->uv[o];
-    a.face_o = s->face[o];
     a.ids_o = s->ids[o];
     a.vel_o = (R2<real>*)s->vel[o];
     a.cnt_o = s->cnt[o];
@@ -335,13 +389,17 @@ void launch_one_step(tds_sim* s, const real* noise) {
     a.perm = s->perm;
     a.start = s->start;
     a.count = s->count;
+    a.tile_sum = s->tile_sum;
+    a.n_tiles = s->n_tiles;
     a.rec = (const real*)s->rec;
+    a.adj = s->adj;
     a.G = s->G;
     a.bin_start = s->bin_start;
     a.bin_faces = s->bin_faces;
+    a.rows = s->rows;
+    a.ivals = s->ivals;
     a.reps = (const RepParams<real>*)s->reps;
     a.local_bits = s->local_bits;
-    a.ox = (real)s->origin[0], a.oy = (real)s->origin[1], a.oz = (real)s->origin[2];
     a.cx = (real)s->mesh->t.centroid[0], a.cy = (real)s->mesh->t.centroid[1], a.cz = (real)s->mesh->t.centroid[2];
     a.noise = noise;
     a.phi_acc = s->phi_acc;
@@ -356,7 +414,7 @@ void launch_one_step(tds_sim* s, const real* noise) {
     }
     {
         KernelTimer kt(s, 3);
-        tdsk::k_finalize<real><<<(s->R + 127) / 128, 128, 0, st>>>(
+        tdsk::k_finalize<real><<<s->R, 128, 0, st>>>(
             s->phi_acc, (const RepParams<real>*)s->reps, s->R, s->series, 0, s->series_cap, s->d_step);
     }
     s->cur = o;
@@ -433,14 +491,15 @@ int load_state(tds_sim* s, const tds_state_view* in) {
     s->cur = 0;
     const int nb = (s->N + 255) / 256;
     tdsk::k_load_state<real><<<nb, 256, 0, s->stream>>>(
-        d_uv, d_th, d_face, d_r3, in->face != nullptr, in->r3d != nullptr, (const real*)s->rec, s->G, s->bin_start,
-        s->bin_faces, s->packed_ids, (R4<real>*)s->pos[0], (R2<real>*)s->uv[0], s->face[0], s->ids[0],
-        (R2<real>*)s->vel[0], s->cnt[0], s->N, s->status);
+        d_uv, d_th, d_face, d_r3, in->face != nullptr, in->r3d != nullptr, (const real*)s->rec, s->adj, s->G,
+        s->bin_start, s->bin_faces, s->packed_ids, (R4<real>*)s->pos[0], (R4<real>*)s->pol[0], (R2<real>*)s->uv[0],
+        s->ids[0], (R2<real>*)s->vel[0], s->cnt[0], s->N, s->status);
     CK(cudaMemsetAsync(s->count, 0, (size_t)s->M * sizeof(int), s->stream));
+    CK(cudaMemsetAsync(s->tile_sum, 0, (size_t)2 * s->n_tiles * sizeof(int), s->stream));
     tdsk::k_prime<real><<<nb, 256, 0, s->stream>>>((const R4<real>*)s->pos[0], s->ids[0],
-                                                    (const RepParams<real>*)s->reps, s->local_bits,
-                                                    (real)s->origin[0], (real)s->origin[1], (real)s->origin[2],
-                                                    s->count, s->key[0], s->rank[0], s->N);
+                                                    (const RepParams<real>*)s->reps, s->local_bits, s->rows,
+                                                    s->ivals, s->count, s->tile_sum, s->n_tiles, s->d_step,
+                                                    s->key[0], s->rank[0], s->N, s->status);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s->stream));
     return TDS_OK;
@@ -458,8 +517,9 @@ int save_state(tds_sim* s, tds_state_view* out) {
     const int c = s->cur;
     const int nb = (s->N + 255) / 256;
     tdsk::k_gather_state<real><<<nb, 256, 0, s->stream>>>(
-        (const R4<real>*)s->pos[c], (const R2<real>*)s->uv[c], s->face[c], s->ids[c], (const R2<real>*)s->vel[c],
-        s->cnt[c], (const RepParams<real>*)s->reps, s->local_bits, d_uv, d_th, d_face, d_r3, d_vel, d_cnt, s->N);
+        (const R4<real>*)s->pos[c], (const R4<real>*)s->pol[c], (const R2<real>*)s->uv[c], s->ids[c],
+        (const R2<real>*)s->vel[c], s->cnt[c], (const RepParams<real>*)s->reps, s->local_bits, d_uv, d_th, d_face, d_r3,
+        d_vel, d_cnt, s->N);
     CK(cudaGetLastError());
     if (out->uv) CK(cudaMemcpyAsync(out->uv, d_uv, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     if (out->theta) CK(cudaMemcpyAsync(out->theta, d_th, N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));

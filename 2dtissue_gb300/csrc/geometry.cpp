@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <unordered_map>
 
 #include "philox.cuh"
 
@@ -50,15 +51,15 @@ void build_face_tables(const Mesh& m, FaceTables& t) {
         const double nn = std::sqrt(nx * nx + ny * ny + nz * nz);
         r[12] = nx / nn, r[13] = ny / nn, r[14] = nz / nn;
         r[16] = a[0], r[17] = a[1], r[18] = b[0], r[19] = b[1], r[20] = c[0], r[21] = c[1];
-        r[22] = A[0], r[23] = A[1], r[24] = A[2];
+        r[24] = A[0], r[25] = A[1], r[26] = A[2];
         const double* P[3] = {a, b, c};
         int bits = 0;
         for (int k = 0; k < 3; ++k) {
             const double ex = P[(k + 1) % 3][0] - P[k][0], ey = P[(k + 1) % 3][1] - P[k][1];
-            r[25 + k] = 1.0 / std::sqrt(ex * ex + ey * ey);
+            r[28 + k] = 1.0 / std::sqrt(ex * ex + ey * ey);
             if (tu[k] > tu[(k + 1) % 3]) bits |= 1 << k;
         }
-        r[28] = (double)bits;
+        r[22] = (double)bits;
         acc += 0.5 * nn;
         t.area_cdf[f] = acc;
     }
@@ -110,26 +111,114 @@ void build_face_tables(const Mesh& m, FaceTables& t) {
     for (int k = 0; k < 3; ++k) t.centroid[k] /= m.V();
 }
 
-static int ceil_log2(int64_t x) {
-    int l = 0;
-    while (((int64_t)1 << l) < x) ++l;
-    return l;
+void build_face_adjacency(const Mesh& m, std::vector<int>& adj) {
+    const int F = m.F();
+    adj.assign((size_t)3 * F, -1);
+    std::unordered_map<uint64_t, int> dir;
+    dir.reserve((size_t)3 * F);
+    for (int f = 0; f < F; ++f)
+        for (int k = 0; k < 3; ++k) {
+            const uint32_t a = (uint32_t)m.fuv[3 * f + k], b = (uint32_t)m.fuv[3 * f + (k + 1) % 3];
+            dir[((uint64_t)a << 32) | b] = 3 * f + k;
+        }
+    for (int f = 0; f < F; ++f)
+        for (int k = 0; k < 3; ++k) {
+            const uint32_t a = (uint32_t)m.fuv[3 * f + k], b = (uint32_t)m.fuv[3 * f + (k + 1) % 3];
+            auto it = dir.find(((uint64_t)b << 32) | a);
+            if (it != dir.end()) adj[3 * f + k] = it->second / 3;
+        }
 }
 
-Fold choose_fold(int n, const FaceTables& t, double h) {
-    Fold fo;
-    int L = std::max(6, ceil_log2(2 * (int64_t)std::max(n, 1)));
-    int g[3];
-    for (int k = 0; k < 3; ++k) g[k] = (int)std::ceil((t.hi[k] - t.lo[k]) / h) + 5;
-    // Largest axis first, each fold at least 4 (distinct buckets for a 3-cell run).
-    int lx = std::min(ceil_log2(g[0]), L - 4);
-    lx = std::max(lx, 2);
-    int ly = std::min(ceil_log2(g[1]), L - lx - 2);
-    ly = std::max(ly, 2);
-    int lz = std::max(2, L - lx - ly);
-    fo.lx = lx, fo.ly = ly, fo.lz = lz;
-    fo.M = (int64_t)1 << (lx + ly + lz);
-    return fo;
+namespace {
+
+// Triangle / axis-aligned box overlap by the separating-axis theorem: the box normals, the
+// triangle normal and the nine cross products of box axes with triangle edges.
+bool tri_box_overlap(const double c[3], const double hw[3], const double* v0, const double* v1, const double* v2) {
+    double a[3], b[3], d[3];
+    for (int k = 0; k < 3; ++k) a[k] = v0[k] - c[k], b[k] = v1[k] - c[k], d[k] = v2[k] - c[k];
+    const double* v[3] = {a, b, d};
+    for (int k = 0; k < 3; ++k) {
+        double mn = std::min(a[k], std::min(b[k], d[k])), mx = std::max(a[k], std::max(b[k], d[k]));
+        if (mn > hw[k] || mx < -hw[k]) return false;
+    }
+    double e[3][3];
+    for (int k = 0; k < 3; ++k) e[0][k] = b[k] - a[k], e[1][k] = d[k] - b[k], e[2][k] = a[k] - d[k];
+    const double nrm[3] = {e[0][1] * e[1][2] - e[0][2] * e[1][1], e[0][2] * e[1][0] - e[0][0] * e[1][2],
+                           e[0][0] * e[1][1] - e[0][1] * e[1][0]};
+    {
+        const double p = nrm[0] * a[0] + nrm[1] * a[1] + nrm[2] * a[2];
+        const double r = hw[0] * std::fabs(nrm[0]) + hw[1] * std::fabs(nrm[1]) + hw[2] * std::fabs(nrm[2]);
+        if (std::fabs(p) > r) return false;
+    }
+    for (int i = 0; i < 3; ++i)      // box axis
+        for (int j = 0; j < 3; ++j) {  // triangle edge
+            double ax[3] = {0, 0, 0};
+            // axis = unit_i x e_j
+            const int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+            ax[i1] = -e[j][i2];
+            ax[i2] = e[j][i1];
+            double mn = 1e300, mx = -1e300;
+            for (int t = 0; t < 3; ++t) {
+                const double p = ax[0] * v[t][0] + ax[1] * v[t][1] + ax[2] * v[t][2];
+                mn = std::min(mn, p), mx = std::max(mx, p);
+            }
+            const double r = hw[0] * std::fabs(ax[0]) + hw[1] * std::fabs(ax[1]) + hw[2] * std::fabs(ax[2]);
+            if (mn > r || mx < -r) return false;
+        }
+    return true;
+}
+
+}  // namespace
+
+void build_cell_level(const Mesh& m, double h, const double origin[3], CellLevel& L) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300}, amax = 0;
+    for (int i = 0; i < m.V(); ++i)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], m.v3[3 * i + k]), hi[k] = std::max(hi[k], m.v3[3 * i + k]);
+            amax = std::max(amax, std::fabs(m.v3[3 * i + k]));
+        }
+    L.h = h;
+    L.gx = (int)std::ceil((hi[0] - origin[0]) / h) + 3;
+    L.gy = (int)std::ceil((hi[1] - origin[1]) / h) + 3;
+    L.gz = (int)std::ceil((hi[2] - origin[2]) / h) + 3;
+    // Cells are widened by eps so that a position rounded to FP32 (error ~ 2^-23 |r|) always
+    // falls into a listed cell.
+    const double eps = 1e-5 * (amax + h);
+    const double hw[3] = {0.5 * h + eps, 0.5 * h + eps, 0.5 * h + eps};
+    std::vector<int64_t> keys;
+    for (int f = 0; f < m.F(); ++f) {
+        const double* p[3] = {&m.v3[3 * m.f3[3 * f]], &m.v3[3 * m.f3[3 * f + 1]], &m.v3[3 * m.f3[3 * f + 2]]};
+        int c0[3], c1[3];
+        for (int k = 0; k < 3; ++k) {
+            double mn = std::min(p[0][k], std::min(p[1][k], p[2][k])), mx = std::max(p[0][k], std::max(p[1][k], p[2][k]));
+            c0[k] = (int)std::floor((mn - eps - origin[k]) / h);
+            c1[k] = (int)std::floor((mx + eps - origin[k]) / h);
+        }
+        for (int iz = c0[2]; iz <= c1[2]; ++iz)
+            for (int iy = c0[1]; iy <= c1[1]; ++iy)
+                for (int ix = c0[0]; ix <= c1[0]; ++ix) {
+                    const double cc[3] = {origin[0] + (ix + 0.5) * h, origin[1] + (iy + 0.5) * h,
+                                          origin[2] + (iz + 0.5) * h};
+                    if (tri_box_overlap(cc, hw, p[0], p[1], p[2]))
+                        keys.push_back(((int64_t)iz * L.gy + iy) * L.gx + ix);
+                }
+    }
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    L.C = (int)keys.size();
+    L.rows.assign((size_t)2 * L.gy * L.gz, 0);
+    L.ivals.clear();
+    for (size_t i = 0; i < keys.size();) {
+        const int64_t row = keys[i] / L.gx;
+        const int x0 = (int)(keys[i] % L.gx);
+        size_t j = i + 1;
+        while (j < keys.size() && keys[j] == keys[j - 1] + 1 && keys[j] / L.gx == row) ++j;
+        const int x1 = x0 + (int)(j - i) - 1;
+        if (L.rows[2 * row + 1] == 0) L.rows[2 * row] = (int)(L.ivals.size() / 4);
+        L.rows[2 * row + 1] += 1;
+        L.ivals.insert(L.ivals.end(), {x0, x1, (int)i, 0});
+        i = j;
+    }
 }
 
 void init_particles(const Mesh& m, const FaceTables& t, int n, uint64_t seed, uint32_t rep, double* uv,
@@ -153,7 +242,7 @@ void init_particles(const Mesh& m, const FaceTables& t, int n, uint64_t seed, ui
         uv[2 * i] = pu, uv[2 * i + 1] = pv;
         face[i] = f;
         const double du = pu - r[16], dv = pv - r[17];
-        for (int k = 0; k < 3; ++k) r3d[3 * i + k] = r[22 + k] + r[k] * du + r[3 + k] * dv;
+        for (int k = 0; k < 3; ++k) r3d[3 * i + k] = r[24 + k] + r[k] * du + r[3 + k] * dv;
         // face frame: e1 along B - A, e2 = n x e1
         const int* t3 = &m.f3[3 * f];
         double e1[3], nrm = 0;

@@ -8,15 +8,15 @@
 
 namespace tds {
 
-// Per-face record, 32 reals (one 128-byte line in FP32):
+// Per-face record, 32 reals (one 128-byte line in FP32), grouped by use in the step kernel:
 //   [0..5]   J   = dX/d(uv), column u = [0..2], column v = [3..5]
 //   [6..11]  Jp  = (J^T J)^-1 J^T, row 0 = [6..8], row 1 = [9..11]
 //   [12..14] n   = unit normal of the 3D triangle (outward)
 //   [16..21] UV corners a, b, c (CCW)
-//   [22..24] 3D corner A (image of a)
-//   [25..27] 1 / UV edge length of edges a->b, b->c, c->a
-//   [28]     canonical-orientation bits: bit k set when edge k runs from the higher to the
+//   [22]     canonical-orientation bits: bit k set when edge k runs from the higher to the
 //            lower chart-vertex id (its orientation value is evaluated reversed and negated)
+//   [24..26] 3D corner A (image of a)
+//   [28..30] 1 / UV edge length of edges a->b, b->c, c->a
 constexpr int kFaceRec = 32;
 
 struct FaceTables {
@@ -32,13 +32,24 @@ struct FaceTables {
 
 void build_face_tables(const Mesh& m, FaceTables& t);
 
-// Folded cell grid for one replica: bucket = base + (ix & (2^lx-1)) | (iy & (2^ly-1)) << lx
-//                                              | (iz & (2^lz-1)) << (lx+ly)
-struct Fold {
-    int lx = 2, ly = 2, lz = 2;
-    int64_t M = 64;
+// Chart edge adjacency: for face f, edge k (corner k -> k+1) borders face adj[3f+k]
+// (-1 on the square's boundary).
+void build_face_adjacency(const Mesh& m, std::vector<int>& adj);
+
+// Compact surface-cell list of one cell size h. Particles always lie on the mesh, so the only
+// cells that can hold particles are those the triangles pass through; they are numbered in
+// (iz, iy, ix) order, so the cells of one x-row that are consecutive in x have consecutive ids.
+// A row (iy, iz) lists its x-intervals; rows[r] = (first interval, count), intervals are
+// (x_lo, x_hi, id of x_lo, 0). Cells are found exactly: no hashing, no collisions.
+struct CellLevel {
+    double h = 0;
+    int gx = 0, gy = 0, gz = 0;
+    int C = 0;  // number of surface cells
+    std::vector<int> rows;   // 2 per row: first interval, count
+    std::vector<int> ivals;  // 4 per interval
 };
-Fold choose_fold(int n_particles, const FaceTables& t, double h);
+// origin: grid corner (mesh bounding box minus a margin of >= 2 cells).
+void build_cell_level(const Mesh& m, double h, const double origin[3], CellLevel& L);
 
 // Seeded placement: face picked with probability proportional to its 3D area, uniform
 // barycentric position, polarity angle uniform in [0, 2pi) in the face frame

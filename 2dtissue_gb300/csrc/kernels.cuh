@@ -1,16 +1,24 @@
-// sm_103a kernels of the per-step particle update (model form; see the design doc for the contract).
+// sm_103a kernels of the per-step particle update.
 //
 // One step is four launches on the handle's stream (captured in a CUDA graph by the host):
-//   k_scan     single-pass exclusive scan of the cell-list counts (decoupled look-back)
+//   k_scan     exclusive scan of the cell-list counts; block bases from per-tile counts that the
+//              previous step accumulated (no inter-block waiting)
 //   k_scatter  counting-sort scatter: perm[start[key] + rank] = slot
-//   k_step     fused pair sums + tangent projection + polarity update + UV advance + seam wrap
-//              + face location + UV->3D map + next-step cell key/count + order-parameter partials
+//   k_step     fused pair sums + tangent projection + polarity update + chart advance + seam
+//              wrap + face location + chart->3D map + next-step cell key/count + order partials
 //   k_finalize order parameter per replica for this step
 // Replaces (reference): Locomotion::simulate_flight + ForceHelper + OrientationHelper
 // (Locomotion.cpp:57-162, ForceHelper.cpp:34-104, OrientationHelper.cpp:29-116),
 // EuclideanTiling::diagonal_seam_edges_square_border (EuclideanTiling.cpp:31-208),
 // CellHelper::get_r3d (CellHelper.cpp:71-160), Validation (Validation.cpp:40-72),
 // count_particle_neighbors (2DTissue.cpp:254-268), calculate_order_parameter (LinearAlgebra.cpp:90-105).
+//
+// State per particle (structure of arrays, in the order of the previous step's cell sort):
+//   pos = (x, y, z, theta)  3D position and chart polarity angle
+//   pol = (px, py, pz, face) unit 3D polarity normalize(J_face (cos theta, sin theta)) and the
+//                            containing chart face (stored with the polarity so that a
+//                            neighbour's polarity is one load)
+//   uv, id
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -25,15 +33,14 @@ enum : int {
     ST_LOCATE = 4,
     ST_NBR = 8,
     ST_CELL = 16,
-    ST_SCAN_TIMEOUT = 32,
 };
 
 constexpr int kRec = 32;          // reals per face record
 constexpr int kMaxWraps = 8;      // seam wraps per particle per step
 constexpr int kNbrMax = 1024;     // neighbours covered by the fixed-point range
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 16;
-constexpr int kScanTile = kScanThreads * kScanItems;
+constexpr int kScanItems = 32;
+constexpr int kScanTile = kScanThreads * kScanItems;  // buckets per scan tile
 constexpr int kStepThreads = 256;
 constexpr int kPhiCopies = 16;    // spread the order-parameter atomics over copies
 constexpr double kPolScale = 1125899906842624.0;  // 2^50: fixed point of neighbour polarity sums
@@ -47,28 +54,30 @@ struct alignas(2 * sizeof(real)) R2 {
     real x, y;
 };
 
-// Per-replica parameters (device copy).
+// Per-replica parameters and the replica's cell level (device copy).
 template <typename real>
 struct RepParams {
     real twoR, inv_twoR, k, adh_scale;  // adh_scale = k_adh / (r_max - 2R)
     real r_max2, v0, mu, inv_tau;
     real align, eta, dt, inv_h;
-    real fscale, inv_fscale, pad0, pad1;  // force fixed point 2^S, 2^-S
+    real fscale, inv_fscale, ox, oy;      // force fixed point 2^S, 2^-S; cell-grid origin
+    real oz, pad0, pad1, pad2;
     double phiscale;                      // order-parameter fixed point
     double inv_n;                         // 1 / particles in this replica
-    int force_mode, base, lx, ly;
-    int lz, n, off, pad3;  // off: global index of the replica's first particle
+    int force_mode, base, C, gx;          // bucket base, surface cells, grid size
+    int gy, gz, row_off, n;               // row table offset of the level
+    int off, pad3, pad4, pad5;            // off: global index of the replica's first particle
 };
 
 template <typename real>
 struct StepArgs {
-    const R4<real>* pos;  // (x, y, z, theta) in physical order
+    const R4<real>* pos;
+    const R4<real>* pol;
     const R2<real>* uv;
-    const int* face;
     const int* ids;
-    R4<real>* pos_o;      // outputs in this step's sorted order
+    R4<real>* pos_o;  // outputs in this step's sorted order
+    R4<real>* pol_o;
     R2<real>* uv_o;
-    int* face_o;
     int* ids_o;
     R2<real>* vel_o;
     int* cnt_o;
@@ -77,15 +86,19 @@ struct StepArgs {
     const int* perm;
     const int* start;
     int* count;
+    int* tile_sum;  // [2][n_tiles]
+    int n_tiles;
     const real* rec;
+    const int4* adj;
     int G;
     const int* bin_start;
     const int* bin_faces;
+    const int2* rows;
+    const int4* ivals;
     const RepParams<real>* reps;
     int local_bits;
-    real ox, oy, oz;
     real cx, cy, cz;
-    const real* noise;  // nullable: angle increments by particle id
+    const real* noise;  // nullable: angle increments by global particle index
     unsigned long long* phi_acc;
     const long long* d_step;
     unsigned long long seed;
@@ -114,10 +127,24 @@ __device__ __forceinline__ float from_fix(long long v, float inv) { return __ll2
 __device__ __forceinline__ double from_fix(long long v, double inv) { return __ll2double_rn(v) * inv; }
 __device__ __forceinline__ bool is_finite(float x) { return isfinite(x); }
 __device__ __forceinline__ bool is_finite(double x) { return isfinite(x); }
+__device__ __forceinline__ float face_to_real(int f, float) { return __int_as_float(f); }
+__device__ __forceinline__ double face_to_real(int f, double) { return (double)f; }
+__device__ __forceinline__ int real_to_face(float v) { return __float_as_int(v); }
+__device__ __forceinline__ int real_to_face(double v) { return (int)v; }
 
 template <typename real>
 __device__ __forceinline__ real kPi() {
     return (real)3.14159265358979323846;
+}
+
+// unit 3D polarity from the chart angle on face record g: normalize(J (cos th, sin th))
+template <typename real>
+__device__ __forceinline__ void polarity3(const real* g, real th, real& px, real& py, real& pz) {
+    real sn, cs;
+    d_sincos(th, &sn, &cs);
+    const real qx = g[0] * cs + g[3] * sn, qy = g[1] * cs + g[4] * sn, qz = g[2] * cs + g[5] * sn;
+    const real qn = d_sqrt(qx * qx + qy * qy + qz * qz);
+    px = qx / qn, py = qy / qn, pz = qz / qn;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -129,7 +156,7 @@ __device__ __forceinline__ real orient(real Px, real Py, real Qx, real Qy, real 
 }
 template <typename real>
 __device__ __forceinline__ void edge_values(const real* r, real px, real py, real e[3]) {
-    const int bits = (int)r[28];
+    const int bits = (int)r[22];
     const real P[3][2] = {{r[16], r[17]}, {r[18], r[19]}, {r[20], r[21]}};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -148,20 +175,26 @@ template <typename real>
 __device__ __forceinline__ real face_score(const real* r, real px, real py) {
     real e[3];
     edge_values(r, px, py, e);
-    return fmin(e[0] * r[25], fmin(e[1] * r[26], e[2] * r[27]));
+    return fmin(e[0] * r[28], fmin(e[1] * r[29], e[2] * r[30]));
 }
 template <typename real>
 __device__ __forceinline__ int bin_coord(real x, int G) {
     int b = (int)d_floor(x * (real)G);
     return b < 0 ? 0 : (b >= G ? G - 1 : b);
 }
-// 1. keep f_old if strictly inside; 2. lowest-index closed-containing face; 3. best score.
+// 1. keep f_old if strictly inside; 2. an edge-neighbour of f_old that strictly contains p;
+// 3. lowest-index closed-containing face; 4. best score (nearest face).
 template <typename real>
-__device__ int locate(const real* rec, int G, const int* bs, const int* bf, real px, real py, int f_old,
-                      int& mode) {
-    if (min_edge(rec + (size_t)f_old * kRec, px, py) > (real)0) {
-        mode = 0;
-        return f_old;
+__device__ int locate(const real* rec, const int4* adj, int G, const int* bs, const int* bf, real px, real py,
+                      int f_old, int& mode) {
+    mode = 0;
+    if (min_edge(rec + (size_t)f_old * kRec, px, py) > (real)0) return f_old;
+    if (adj) {
+        const int4 A = adj[f_old];
+        const int nb[3] = {A.x, A.y, A.z};
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            if (nb[k] >= 0 && min_edge(rec + (size_t)nb[k] * kRec, px, py) > (real)0) return nb[k];
     }
     const int bx = bin_coord(px, G), by = bin_coord(py, G);
     const int b = by * G + bx;
@@ -273,95 +306,118 @@ __device__ __forceinline__ real norm_angle(real th) {
     return th;
 }
 
-// folded cell-grid bucket of a position
+// ---------------------------------------------------------------------------------------------
+// compact surface-cell list
+// ---------------------------------------------------------------------------------------------
 template <typename real>
-__device__ __forceinline__ int bucket_of(const RepParams<real>& rp, real x, real y, real z, real ox, real oy,
-                                         real oz) {
-    const int ix = (int)d_floor((x - ox) * rp.inv_h), iy = (int)d_floor((y - oy) * rp.inv_h),
-              iz = (int)d_floor((z - oz) * rp.inv_h);
-    const unsigned mx = (1u << rp.lx) - 1u, my = (1u << rp.ly) - 1u, mz = (1u << rp.lz) - 1u;
-    return rp.base + (int)(((unsigned)ix & mx) | (((unsigned)iy & my) << rp.lx) |
-                           (((unsigned)iz & mz) << (rp.lx + rp.ly)));
+__device__ __forceinline__ void cell_coords(const RepParams<real>& rp, real x, real y, real z, int& ix, int& iy,
+                                            int& iz) {
+    // clamped into the grid interior so that every lookup stays in bounds (positions on the mesh
+    // are at least two cells inside; NaN converts to 0 and is clamped)
+    ix = min(max((int)d_floor((x - rp.ox) * rp.inv_h), 1), rp.gx - 2);
+    iy = min(max((int)d_floor((y - rp.oy) * rp.inv_h), 1), rp.gy - 2);
+    iz = min(max((int)d_floor((z - rp.oz) * rp.inv_h), 1), rp.gz - 2);
+}
+// bucket of a position: base + surface-cell id, or base + C when the cell is not a surface cell
+template <typename real>
+__device__ __forceinline__ int bucket_of(const RepParams<real>& rp, const int2* rows, const int4* ivals, real x,
+                                         real y, real z, bool& lost) {
+    int ix, iy, iz;
+    cell_coords(rp, x, y, z, ix, iy, iz);
+    const int2 R = rows[rp.row_off + iz * rp.gy + iy];
+    for (int k = 0; k < R.y; ++k) {
+        const int4 I = ivals[R.x + k];
+        if (ix >= I.x && ix <= I.y) {
+            lost = false;
+            return rp.base + I.z + ix - I.x;
+        }
+    }
+    lost = true;
+    return rp.base + rp.C;
+}
+
+__device__ __forceinline__ void add_tile(int* tile_sum, int key) {
+    // warp-aggregated count of keys per scan tile
+    const int tile = key / kScanTile;
+    const unsigned m = __match_any_sync(__activemask(), tile);
+    if ((threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(&tile_sum[tile], __popc(m));
 }
 
 // ---------------------------------------------------------------------------------------------
 // k_step
 // ---------------------------------------------------------------------------------------------
 template <typename real>
-__global__ void __launch_bounds__(kStepThreads) k_step(const StepArgs<real> a) {
+__global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs<real> a) {
     typedef R4<real> r4;
     const int q = blockIdx.x * kStepThreads + threadIdx.x;
     const bool active = q < a.N;
     int rep = -1;
     long long ph[6] = {0, 0, 0, 0, 0, 0};
     int st = 0;
+    const long long step = *a.d_step;
     if (active) {
         const int s = a.perm[q];
         const r4 P = a.pos[s];
+        const r4 PL = a.pol[s];
         const R2<real> U = a.uv[s];
-        const int f = a.face[s];
         const int id = a.ids[s];
+        const int f = real_to_face(PL.w);
         rep = (int)((unsigned)id >> a.local_bits);
         const unsigned local = (unsigned)id & ((1u << a.local_bits) - 1u);
-        const RepParams<real> rp = a.reps[rep];
+        const RepParams<real>& rp = a.reps[rep];
         const real* g = a.rec + (size_t)f * kRec;
-        const real J0 = g[0], J1 = g[1], J2 = g[2], J3 = g[3], J4 = g[4], J5 = g[5];
-        const real nx = g[12], ny = g[13], nz = g[14];
-        // own polarity: p = normalize(J (cos th, sin th))
-        real sn, cs;
-        d_sincos(P.w, &sn, &cs);
-        real qx = J0 * cs + J3 * sn, qy = J1 * cs + J4 * sn, qz = J2 * cs + J5 * sn;
-        real qn = d_sqrt(qx * qx + qy * qy + qz * qz);
-        const real px = qx / qn, py = qy / qn, pz = qz / qn;
+        const real px = PL.x, py = PL.y, pz = PL.z;
+        const real r_max2 = rp.r_max2, twoR = rp.twoR;
 
-        // pair sums over the 27 cells around the particle (9 runs of 3 consecutive buckets)
+        // candidate ranges: 9 rows (dy, dz) x 3 consecutive cells in x
+        int ix, iy, iz;
+        cell_coords(rp, P.x, P.y, P.z, ix, iy, iz);
+        int t0[9], t1[9];
+#pragma unroll
+        for (int r = 0; r < 9; ++r) {
+            const int2 R = a.rows[rp.row_off + (iz + r / 3 - 1) * rp.gy + (iy + r % 3 - 1)];
+            int ida = 0x7fffffff, idb = -1;
+            for (int k = 0; k < R.y; ++k) {
+                const int4 I = a.ivals[R.x + k];
+                const int lo = max(I.x, ix - 1), hi = min(I.y, ix + 1);
+                if (lo <= hi) {
+                    ida = min(ida, I.z + lo - I.x);
+                    idb = max(idb, I.z + hi - I.x);
+                }
+            }
+            if (ida <= idb) {
+                t0[r] = a.start[rp.base + ida];
+                t1[r] = a.start[rp.base + idb + 1];
+            } else {
+                t0[r] = 0, t1[r] = 0;
+            }
+        }
+        // pair sums (fixed point: the sum is independent of the neighbour order)
         long long Fx = 0, Fy = 0, Fz = 0, Mx = 0, My = 0, Mz = 0;
         int cnt = 0;
         const real pscale = (real)kPolScale;
-        auto pair = [&](int j) {
-            if (j == s) return;
-            const r4 Q = a.pos[j];
-            const real dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
-            const real d2 = dx * dx + dy * dy + dz * dz;
-            if (!(d2 < rp.r_max2)) return;
-            const real d = d_sqrt(d2);
-            const real fm = d < rp.twoR ? rp.k * (rp.twoR - d) * rp.inv_twoR : -(rp.adh_scale * (d - rp.twoR));
-            if (d > (real)0) {
-                const real c = fm / d;
-                Fx += to_fix(c * dx, rp.fscale);
-                Fy += to_fix(c * dy, rp.fscale);
-                Fz += to_fix(c * dz, rp.fscale);
-            }
-            const int fj = a.face[j];
-            const real* gj = a.rec + (size_t)fj * kRec;
-            real sj, cj;
-            d_sincos(Q.w, &sj, &cj);
-            const real ux = gj[0] * cj + gj[3] * sj, uy = gj[1] * cj + gj[4] * sj, uz = gj[2] * cj + gj[5] * sj;
-            const real un = d_sqrt(ux * ux + uy * uy + uz * uz);
-            Mx += to_fix(ux / un, pscale);
-            My += to_fix(uy / un, pscale);
-            Mz += to_fix(uz / un, pscale);
-            ++cnt;
-        };
-        {
-            const int ix = (int)d_floor((P.x - a.ox) * rp.inv_h), iy = (int)d_floor((P.y - a.oy) * rp.inv_h),
-                      iz = (int)d_floor((P.z - a.oz) * rp.inv_h);
-            const unsigned mxk = (1u << rp.lx) - 1u, myk = (1u << rp.ly) - 1u, mzk = (1u << rp.lz) - 1u;
-            const unsigned Px = mxk + 1u;
-            const unsigned x0 = (unsigned)(ix - 1) & mxk;
-            for (int dz = -1; dz <= 1; ++dz) {
-                const unsigned rz = ((unsigned)(iz + dz) & mzk) << (rp.lx + rp.ly);
-                for (int dy = -1; dy <= 1; ++dy) {
-                    const int row = rp.base + (int)(rz | (((unsigned)(iy + dy) & myk) << rp.lx));
-                    if (x0 + 3u <= Px) {
-                        const int e = a.start[row + x0 + 3];
-                        for (int t = a.start[row + x0]; t < e; ++t) pair(a.perm[t]);
-                    } else {
-                        const int e0 = a.start[row + Px];
-                        for (int t = a.start[row + x0]; t < e0; ++t) pair(a.perm[t]);
-                        const int e1 = a.start[row + x0 + 3 - Px];
-                        for (int t = a.start[row]; t < e1; ++t) pair(a.perm[t]);
+#pragma unroll 1
+        for (int r = 0; r < 9; ++r) {
+#pragma unroll 2
+            for (int t = t0[r]; t < t1[r]; ++t) {
+                const int j = a.perm[t];
+                const r4 Q = a.pos[j];
+                const real dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
+                const real d2 = dx * dx + dy * dy + dz * dz;
+                if (d2 < r_max2 && j != s) {
+                    const r4 QL = a.pol[j];
+                    const real d = d_sqrt(d2);
+                    const real fm = d < twoR ? rp.k * (twoR - d) * rp.inv_twoR : -(rp.adh_scale * (d - twoR));
+                    if (d > (real)0) {
+                        const real c = fm / d;
+                        Fx += to_fix(c * dx, rp.fscale);
+                        Fy += to_fix(c * dy, rp.fscale);
+                        Fz += to_fix(c * dz, rp.fscale);
                     }
+                    Mx += to_fix(QL.x, pscale);
+                    My += to_fix(QL.y, pscale);
+                    Mz += to_fix(QL.z, pscale);
+                    ++cnt;
                 }
             }
         }
@@ -372,6 +428,7 @@ __global__ void __launch_bounds__(kStepThreads) k_step(const StepArgs<real> a) {
         const real mxr = from_fix(Mx, ips), myr = from_fix(My, ips), mzr = from_fix(Mz, ips);
 
         // tangent projection and velocity
+        const real nx = g[12], ny = g[13], nz = g[14];
         const real Fn = Fxr * nx + Fyr * ny + Fzr * nz;
         const real Tx = Fxr - Fn * nx, Ty = Fyr - Fn * ny, Tz = Fzr - Fn * nz;
         real vx, vy, vz;
@@ -381,7 +438,7 @@ __global__ void __launch_bounds__(kStepThreads) k_step(const StepArgs<real> a) {
             const real sp = rp.v0 + d_sqrt(Tx * Tx + Ty * Ty + Tz * Tz);
             vx = sp * px, vy = sp * py, vz = sp * pz;
         }
-        // polarity rotation about n: relaxation to v, alignment to neighbours, noise
+        // polarity rotation about n: relaxation towards v, alignment with neighbours, noise
         const real vn = d_sqrt(vx * vx + vy * vy + vz * vz);
         const real mn = d_sqrt(mxr * mxr + myr * myr + mzr * mzr);
         real omega = (real)0;
@@ -393,7 +450,6 @@ __global__ void __launch_bounds__(kStepThreads) k_step(const StepArgs<real> a) {
             const real cx = py * mzr - pz * myr, cy = pz * mxr - px * mzr, cz = px * myr - py * mxr;
             omega += rp.align * (cx * nx + cy * ny + cz * nz) / mn;
         }
-        const long long step = *a.d_step;
         real xi;
         if (a.noise) {
             xi = a.noise[rp.off + (int)local];
@@ -414,37 +470,42 @@ __global__ void __launch_bounds__(kStepThreads) k_step(const StepArgs<real> a) {
         real vv = g[9] * vx + g[10] * vy + g[11] * vz;
         real u2 = U.x + rp.dt * vu, v2 = U.y + rp.dt * vv;
         int nw = 0;
-        const int wr = seam_wrap(U.x, U.y, u2, v2, th, vu, vv, nw);
-        if (wr) st |= ST_WRAP;
+        if (seam_wrap(U.x, U.y, u2, v2, th, vu, vv, nw)) st |= ST_WRAP;
         th = norm_angle(th);
         int mode = 0;
-        const int f2 = locate(a.rec, a.G, a.bin_start, a.bin_faces, u2, v2, f, mode);
+        const int f2 = locate(a.rec, a.adj, a.G, a.bin_start, a.bin_faces, u2, v2, f, mode);
         if (mode == 2) st |= ST_LOCATE;
         const real* h = a.rec + (size_t)f2 * kRec;
         const real du = u2 - h[16], dv = v2 - h[17];
-        const real rx = h[22] + h[0] * du + h[3] * dv;
-        const real ry = h[23] + h[1] * du + h[4] * dv;
-        const real rz = h[24] + h[2] * du + h[5] * dv;
+        const real rx = h[24] + h[0] * du + h[3] * dv;
+        const real ry = h[25] + h[1] * du + h[4] * dv;
+        const real rz = h[26] + h[2] * du + h[5] * dv;
+        real qx, qy, qz;
+        polarity3(h, th, qx, qy, qz);
         if (!(is_finite(rx) && is_finite(ry) && is_finite(rz) && is_finite(u2) && is_finite(v2) && is_finite(th)))
             st |= ST_NONFINITE;
 
         r4 o;
         o.x = rx, o.y = ry, o.z = rz, o.w = th;
         a.pos_o[q] = o;
+        r4 ol;
+        ol.x = qx, ol.y = qy, ol.z = qz, ol.w = face_to_real(f2, (real)0);
+        a.pol_o[q] = ol;
         R2<real> uo;
         uo.x = u2, uo.y = v2;
         a.uv_o[q] = uo;
-        a.face_o[q] = f2;
         a.ids_o[q] = id;
         R2<real> vo;
         vo.x = vu, vo.y = vv;
         a.vel_o[q] = vo;
         a.cnt_o[q] = cnt;
-        // next step's cell key and rank (counting sort)
-        const int key = bucket_of(rp, rx, ry, rz, a.ox, a.oy, a.oz);
-        const int rank = atomicAdd(&a.count[key], 1);
+        // next step's cell key, rank and scan-tile count (counting sort)
+        bool lost = false;
+        const int key = bucket_of(rp, a.rows, a.ivals, rx, ry, rz, lost);
+        if (lost) st |= ST_CELL;
+        a.rank_o[q] = atomicAdd(&a.count[key], 1);
         a.key_o[q] = key;
-        a.rank_o[q] = rank;
+        add_tile(a.tile_sum + (size_t)((step + 1) & 1) * a.n_tiles, key);
 
         // order-parameter partials: normalize((r' - c) x v), v / |v|
         const real ax = rx - a.cx, ay = ry - a.cy, az = rz - a.cz;
@@ -484,26 +545,27 @@ __global__ void __launch_bounds__(kStepThreads) k_step(const StepArgs<real> a) {
             for (int k = 0; k < 6; ++k) s_ph[warp][k] = ph[k];
         }
     } else {
-        if (active)
+        if (active) {
+#pragma unroll
             for (int k = 0; k < 6; ++k)
                 atomicAdd(&a.phi_acc[((size_t)rep * kPhiCopies + copy) * 6 + k], (unsigned long long)ph[k]);
+        }
         if (lane == 0) s_rep[warp] = -1;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
         int cur = -1;
-        long long acc[6] = {0, 0, 0, 0, 0, 0};
+        long long acc = 0;
         for (int w = 0; w <= kStepThreads / 32; ++w) {
             const int r = (w < kStepThreads / 32) ? s_rep[w] : -2;
             if (r != cur) {
                 if (cur >= 0)
-                    for (int k = 0; k < 6; ++k)
-                        atomicAdd(&a.phi_acc[((size_t)cur * kPhiCopies + copy) * 6 + k], (unsigned long long)acc[k]);
+                    atomicAdd(&a.phi_acc[((size_t)cur * kPhiCopies + copy) * 6 + k], (unsigned long long)acc);
                 cur = r;
-                for (int k = 0; k < 6; ++k) acc[k] = 0;
+                acc = 0;
             }
-            if (r >= 0)
-                for (int k = 0; k < 6; ++k) acc[k] += s_ph[w][k];
+            if (r >= 0) acc += s_ph[w][k];
         }
     }
 }
@@ -511,44 +573,54 @@ __global__ void __launch_bounds__(kStepThreads) k_step(const StepArgs<real> a) {
 // ---------------------------------------------------------------------------------------------
 // cell-list kernels
 // ---------------------------------------------------------------------------------------------
-// Single-pass exclusive scan of count[0..M) into start[0..M), zeroing count. Tiles take a
-// ticket (so every tile waits only on tiles already running) and publish
-// (epoch, flag, value) words; flag 1 = aggregate, 2 = inclusive prefix.
-__device__ __forceinline__ unsigned long long ld_volatile_u64(const unsigned long long* p) {
-    return *(volatile const unsigned long long*)p;
-}
-
+// Exclusive scan of count[0..M) into start[0..M), zeroing count. Each block's base is the sum of
+// the per-tile counts of the tiles before it (accumulated by the previous step), so no block
+// waits on another. Also zeroes the other parity's tile counts for the step about to run.
 __global__ void __launch_bounds__(kScanThreads) k_scan(int* __restrict__ count, int* __restrict__ start, long long M,
-                                                       unsigned long long* tile_state, unsigned* tickets,
-                                                       const long long* d_step, int* status) {
-    __shared__ int s_tile;
+                                                       int* __restrict__ tile_sum, int n_tiles,
+                                                       const long long* d_step) {
     __shared__ int s_warp[kScanThreads / 32];
-    __shared__ int s_excl;
-    const unsigned epoch = (unsigned)((*d_step + 2) & 0x3fffffff);
-    const int slot = (int)(epoch & 1u);
+    __shared__ int s_base;
+    const int par = (int)((*d_step + 1) & 1);
+    const int* ts = tile_sum + (size_t)par * n_tiles;
+    const int tile = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // base = sum of ts[0..tile)
+    int part = 0;
+    for (int i = threadIdx.x; i < tile; i += kScanThreads) part += ts[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0) s_warp[warp] = part;
+    __syncthreads();
     if (threadIdx.x == 0) {
-        s_tile = (int)atomicAdd(&tickets[slot], 1u);
-        if (s_tile == 0) tickets[slot ^ 1] = 0u;
+        int b = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) b += s_warp[w];
+        s_base = b;
+        tile_sum[(size_t)(par ^ 1) * n_tiles + tile] = 0;
     }
     __syncthreads();
-    const int tile = s_tile;
     const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
     int v[kScanItems];
     int sum = 0;
+    if (base + kScanItems <= M) {
 #pragma unroll
-    for (int i = 0; i < kScanItems; ++i) {
-        const long long idx = base + i;
-        v[i] = idx < M ? count[idx] : 0;
-        sum += v[i];
+        for (int i = 0; i < kScanItems; i += 4) {
+            const int4 x = *reinterpret_cast<const int4*>(count + base + i);
+            v[i] = x.x, v[i + 1] = x.y, v[i + 2] = x.z, v[i + 3] = x.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < kScanItems; ++i) v[i] = base + i < M ? count[base + i] : 0;
     }
-    // block exclusive scan of per-thread sums
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) sum += v[i];
     int incl = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const int t = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += t;
     }
+    __syncthreads();
     if (lane == 31) s_warp[warp] = incl;
     __syncthreads();
     if (warp == 0) {
@@ -561,68 +633,31 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(int* __restrict__ count, 
         if (lane < kScanThreads / 32) s_warp[lane] = w;
     }
     __syncthreads();
-    const int tile_total = s_warp[kScanThreads / 32 - 1];
-    const int thread_excl = incl - sum + (warp ? s_warp[warp - 1] : 0);
-    // decoupled look-back (warp 0)
-    if (warp == 0) {
-        const unsigned long long tag = (unsigned long long)epoch << 34;
-        if (lane == 0) {
-            const unsigned long long w =
-                tag | ((unsigned long long)(tile == 0 ? 2u : 1u) << 32) | (unsigned)tile_total;
-            atomicExch(&tile_state[tile], w);
-        }
-        int excl = 0;
-        if (tile > 0) {
-            int idx = tile - 1 - lane;
-            bool done = false;
-            long long spins = 0;
-            while (!done) {
-                unsigned long long w = 0;
-                unsigned flag = 2;
-                unsigned val = 0;
-                if (idx >= 0) {
-                    for (;;) {
-                        w = ld_volatile_u64(&tile_state[idx]);
-                        flag = ((w >> 34) == epoch) ? (unsigned)((w >> 32) & 3u) : 0u;
-                        if (flag != 0) break;
-                        if (++spins > (1ll << 22)) {
-                            atomicOr(status, ST_SCAN_TIMEOUT);
-                            flag = 2;
-                            break;
-                        }
-                        __nanosleep(64);
-                    }
-                    val = (unsigned)w;
-                }
-                const unsigned pmask = __ballot_sync(0xffffffffu, flag == 2);
-                int contrib;
-                if (pmask) {
-                    const int first = __ffs(pmask) - 1;  // nearest predecessor with a prefix
-                    contrib = lane <= first ? (int)val : 0;
-                    done = true;
-                } else {
-                    contrib = (int)val;
-                    idx -= 32;
-                }
+    int run = s_base + incl - sum + (warp ? s_warp[warp - 1] : 0);
+    if (base + kScanItems <= M) {
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(0xffffffffu, contrib, o);
-                excl += contrib;
+        for (int i = 0; i < kScanItems; i += 4) {
+            int4 o;
+            o.x = run;
+            run += v[i];
+            o.y = run;
+            run += v[i + 1];
+            o.z = run;
+            run += v[i + 2];
+            o.w = run;
+            run += v[i + 3];
+            *reinterpret_cast<int4*>(start + base + i) = o;
+            *reinterpret_cast<int4*>(count + base + i) = make_int4(0, 0, 0, 0);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < kScanItems; ++i) {
+            if (base + i < M) {
+                start[base + i] = run;
+                count[base + i] = 0;
             }
-            if (lane == 0)
-                atomicExch(&tile_state[tile], tag | (2ull << 32) | (unsigned)(excl + tile_total));
+            run += v[i];
         }
-        if (lane == 0) s_excl = excl;
-    }
-    __syncthreads();
-    int run = s_excl + thread_excl;
-#pragma unroll
-    for (int i = 0; i < kScanItems; ++i) {
-        const long long idx = base + i;
-        if (idx < M) {
-            start[idx] = run;
-            count[idx] = 0;
-        }
-        run += v[i];
     }
 }
 
@@ -633,48 +668,57 @@ __global__ void k_scatter(const int* __restrict__ key, const int* __restrict__ r
     if (s < N) perm[start[key[s]] + rank[s]] = s;
 }
 
-// Cell keys and ranks of the current state (after start / set_state), counts must be zero.
+// Cell keys, ranks and tile counts of the current state (after start / set_state); counts and
+// tile counts must be zero.
 template <typename real>
-__global__ void k_prime(const R4<real>* pos, const int* ids, const RepParams<real>* reps, int local_bits, real ox,
-                        real oy, real oz, int* count, int* key, int* rank, int N) {
+__global__ void k_prime(const R4<real>* pos, const int* ids, const RepParams<real>* reps, int local_bits,
+                        const int2* rows, const int4* ivals, int* count, int* tile_sum, int n_tiles,
+                        const long long* d_step, int* key, int* rank, int N, int* status) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= N) return;
     const R4<real> P = pos[s];
-    const RepParams<real> rp = reps[(unsigned)ids[s] >> local_bits];
-    const int k = bucket_of(rp, P.x, P.y, P.z, ox, oy, oz);
+    const RepParams<real>& rp = reps[(unsigned)ids[s] >> local_bits];
+    bool lost = false;
+    const int k = bucket_of(rp, rows, ivals, P.x, P.y, P.z, lost);
+    if (lost) atomicOr(status, ST_CELL);
     key[s] = k;
     rank[s] = atomicAdd(&count[k], 1);
+    add_tile(tile_sum + (size_t)((*d_step + 1) & 1) * n_tiles, k);
 }
 
-// Order parameter of the step just taken, per replica; zeroes the accumulators.
+// Order parameter of the step just taken, per replica (one block per replica); zeroes the
+// accumulators.
 template <typename real>
 __global__ void k_finalize(unsigned long long* phi_acc, const RepParams<real>* reps, int R, double* series,
                            long long series_base, long long cap_steps, const long long* d_step) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= R) return;
-    double s[6];
-    for (int k = 0; k < 6; ++k) s[k] = 0;
-    for (int c = 0; c < kPhiCopies; ++c)
-        for (int k = 0; k < 6; ++k) {
-            unsigned long long* p = &phi_acc[((size_t)r * kPhiCopies + c) * 6 + k];
-            s[k] += (double)(long long)(*p);
-            *p = 0ull;
+    __shared__ double s[kPhiCopies * 6];
+    const int r = blockIdx.x;
+    const int t = threadIdx.x;
+    if (t < kPhiCopies * 6) {
+        unsigned long long* p = &phi_acc[(size_t)r * kPhiCopies * 6 + t];
+        s[t] = (double)(long long)(*p);
+        *p = 0ull;
+    }
+    __syncthreads();
+    if (t == 0) {
+        double v[6] = {0, 0, 0, 0, 0, 0};
+        for (int c = 0; c < kPhiCopies; ++c)
+            for (int k = 0; k < 6; ++k) v[k] += s[c * 6 + k];
+        const RepParams<real>& rp = reps[r];
+        const double inv = 1.0 / rp.phiscale;
+        const double phi = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) * inv * rp.inv_n;
+        const double psi = sqrt(v[3] * v[3] + v[4] * v[4] + v[5] * v[5]) * inv * rp.inv_n;
+        const long long tt = *d_step - series_base;
+        if (tt >= 0 && tt < cap_steps) {
+            series[(size_t)tt * 2 * R + r] = phi;
+            series[(size_t)tt * 2 * R + R + r] = psi;
         }
-    const RepParams<real>& rp = reps[r];
-    const double inv = 1.0 / rp.phiscale;
-    const double Lx = s[0] * inv, Ly = s[1] * inv, Lz = s[2] * inv;
-    const double phi = sqrt(Lx * Lx + Ly * Ly + Lz * Lz) * rp.inv_n;
-    const double psi = sqrt(s[3] * s[3] + s[4] * s[4] + s[5] * s[5]) * inv * rp.inv_n;
-    const long long t = *d_step - series_base;
-    if (t >= 0 && t < cap_steps) {
-        series[(size_t)t * 2 * R + r] = phi;
-        series[(size_t)t * 2 * R + R + r] = psi;
     }
 }
 
-// Scatter the state (physical order) into id order, in double.
+// State (physical order) -> id order, in double.
 template <typename real>
-__global__ void k_gather_state(const R4<real>* pos, const R2<real>* uv, const int* face, const int* ids,
+__global__ void k_gather_state(const R4<real>* pos, const R4<real>* pol, const R2<real>* uv, const int* ids,
                                const R2<real>* vel, const int* cnt, const RepParams<real>* reps, int local_bits,
                                double* o_uv, double* o_th, int* o_face, double* o_r3d, double* o_vel, int* o_cnt,
                                int N) {
@@ -686,48 +730,48 @@ __global__ void k_gather_state(const R4<real>* pos, const R2<real>* uv, const in
     const R2<real> U = uv[s];
     o_uv[2 * i] = U.x, o_uv[2 * i + 1] = U.y;
     o_th[i] = P.w;
-    o_face[i] = face[s];
+    o_face[i] = real_to_face(pol[s].w);
     o_r3d[3 * i] = P.x, o_r3d[3 * i + 1] = P.y, o_r3d[3 * i + 2] = P.z;
-    if (vel) {
-        const R2<real> V = vel[s];
-        o_vel[2 * i] = V.x, o_vel[2 * i + 1] = V.y;
-        o_cnt[i] = cnt[s];
-    }
+    const R2<real> V = vel[s];
+    o_vel[2 * i] = V.x, o_vel[2 * i + 1] = V.y;
+    o_cnt[i] = cnt[s];
 }
 
-// Load a state given in id order (double) into physical slots = ids; locate faces that are
-// < 0 and map r3d when it is not given.
+// Loads a state given in id order (double) into slots = global index; locates faces that are
+// < 0, maps r3d when it is not given, derives the 3D polarity.
 template <typename real>
 __global__ void k_load_state(const double* i_uv, const double* i_th, const int* i_face, const double* i_r3d,
-                             int has_face, int has_r3d, const real* rec, int G, const int* bs, const int* bf,
-                             const int* packed_ids, R4<real>* pos, R2<real>* uv, int* face, int* ids, R2<real>* vel,
-                             int* cnt, int N, int* status) {
+                             int has_face, int has_r3d, const real* rec, const int4* adj, int G, const int* bs,
+                             const int* bf, const int* packed_ids, R4<real>* pos, R4<real>* pol, R2<real>* uv,
+                             int* ids, R2<real>* vel, int* cnt, int N, int* status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const real u = (real)i_uv[2 * i], v = (real)i_uv[2 * i + 1];
     int f = has_face ? i_face[i] : -1;
     if (f < 0) {
         int mode = 0;
-        // no previous face: start the search from face 0's test (strict) then the bins
-        f = locate(rec, G, bs, bf, u, v, 0, mode);
+        f = locate<real>(rec, nullptr, G, bs, bf, u, v, 0, mode);
         if (mode == 2) atomicOr(status, ST_LOCATE);
     }
+    const real* h = rec + (size_t)f * kRec;
     R4<real> P;
     if (has_r3d) {
         P.x = (real)i_r3d[3 * i], P.y = (real)i_r3d[3 * i + 1], P.z = (real)i_r3d[3 * i + 2];
     } else {
-        const real* h = rec + (size_t)f * kRec;
         const real du = u - h[16], dv = v - h[17];
-        P.x = h[22] + h[0] * du + h[3] * dv;
-        P.y = h[23] + h[1] * du + h[4] * dv;
-        P.z = h[24] + h[2] * du + h[5] * dv;
+        P.x = h[24] + h[0] * du + h[3] * dv;
+        P.y = h[25] + h[1] * du + h[4] * dv;
+        P.z = h[26] + h[2] * du + h[5] * dv;
     }
     P.w = (real)i_th[i];
     pos[i] = P;
+    R4<real> L;
+    polarity3(h, P.w, L.x, L.y, L.z);
+    L.w = face_to_real(f, (real)0);
+    pol[i] = L;
     R2<real> U;
     U.x = u, U.y = v;
     uv[i] = U;
-    face[i] = f;
     ids[i] = packed_ids[i];
     R2<real> Z;
     Z.x = 0, Z.y = 0;

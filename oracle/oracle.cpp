@@ -115,6 +115,7 @@ struct Face {
 
 struct orc_mesh {
     std::vector<Face> faces;
+    std::vector<int> adj;  // 3 per face: chart face across edge k (corner k -> k+1), -1 on the border
     int G = 1;
     std::vector<int> bin_start, bin_faces;
 };
@@ -145,14 +146,21 @@ inline int bin_coord(double x, int G) {
     return b < 0 ? 0 : (b >= G ? G - 1 : b);
 }
 
-// Model point location rule:
+// Model point location rule (the reference takes the argmin of the point-triangle distance over
+// all faces, lowest index on ties, CellHelper.cpp:104-117; for a point inside the chart that is
+// the containing face):
 //  1. keep f_old if p is strictly inside it;
-//  2. else the lowest-index face that contains p (closed triangle);
-//  3. else the face with the largest minimum signed edge distance (ties -> lowest index).
+//  2. else an edge-neighbour of f_old that strictly contains p (edges in order 0, 1, 2);
+//  3. else the lowest-index face that contains p (closed triangle);
+//  4. else the face with the largest minimum signed edge distance (ties -> lowest index).
 int locate(const orc_mesh& M, double px, double py, int f_old, int* mode) {
-    if (f_old >= 0 && f_old < (int)M.faces.size() && min_edge(M.faces[f_old], px, py) > 0) {
-        if (mode) *mode = 0;
-        return f_old;
+    if (mode) *mode = 0;
+    if (f_old >= 0 && f_old < (int)M.faces.size()) {
+        if (min_edge(M.faces[f_old], px, py) > 0) return f_old;
+        for (int k = 0; k < 3; ++k) {
+            const int g = M.adj[3 * f_old + k];
+            if (g >= 0 && min_edge(M.faces[g], px, py) > 0) return g;
+        }
     }
     const int G = M.G;
     int bx = bin_coord(px, G), by = bin_coord(py, G);
@@ -736,6 +744,20 @@ orc_mesh* orc_mesh_create(int V, const double* v3, int F, const int* f3, int Vuv
             double ex = Cc[(k2 + 1) % 3][0] - Cc[k2][0], ey = Cc[(k2 + 1) % 3][1] - Cc[k2][1];
             g.elen[k2] = std::sqrt(ex * ex + ey * ey);
         }
+    }
+    // chart edge adjacency from the UV triangles
+    M->adj.assign((size_t)3 * F, -1);
+    {
+        std::unordered_map<uint64_t, int> dir;
+        dir.reserve((size_t)3 * F);
+        for (int f = 0; f < F; ++f)
+            for (int k = 0; k < 3; ++k)
+                dir[((uint64_t)(uint32_t)fuv[3 * f + k] << 32) | (uint32_t)fuv[3 * f + (k + 1) % 3]] = f;
+        for (int f = 0; f < F; ++f)
+            for (int k = 0; k < 3; ++k) {
+                auto it = dir.find(((uint64_t)(uint32_t)fuv[3 * f + (k + 1) % 3] << 32) | (uint32_t)fuv[3 * f + k]);
+                if (it != dir.end()) M->adj[3 * f + k] = it->second;
+            }
     }
     // UV bin grid (closed bounding boxes), faces in ascending id per bin.
     int G = (int)std::ceil(std::sqrt((double)F));
