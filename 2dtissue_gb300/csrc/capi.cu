@@ -60,6 +60,7 @@ struct tds_sim {
     int2* rows = nullptr;       // all levels' row tables
     int4* ivals = nullptr;      // all levels' x-intervals
     int4* adj = nullptr;        // chart edge adjacency per face
+    uint4* desc = nullptr;      // per-cell neighbour-run descriptors (3 uint4 per cell)
     int* tile_sum = nullptr;    // [2][n_tiles] per-tile counts (step parity)
     uint64_t seed = 0;
     long long step = 0;  // completed steps
@@ -192,11 +193,17 @@ int upload_tables(tds_sim* s) {
         }
         s->level_of[r] = li;
     }
-    std::vector<int> row_off(levels.size());
+    std::vector<int> row_off(levels.size()), desc_off(levels.size());
     std::vector<int2> rows;
     std::vector<int4> ivals;
+    std::vector<uint32_t> desc;
     for (size_t i = 0; i < levels.size(); ++i) {
         const tds::CellLevel& L = levels[i].L;
+        if (L.C >= (1 << 28)) return fail(s, TDS_ERR_LIMIT, "more than 2^28 surface cells in one level");
+        desc_off[i] = (int)(desc.size() / 4);
+        std::vector<uint32_t> d;
+        tds::build_cell_descriptors(L, d);
+        desc.insert(desc.end(), d.begin(), d.end());
         row_off[i] = (int)rows.size();
         const int ib = (int)ivals.size();
         for (size_t r = 0; r < L.rows.size() / 2; ++r) rows.push_back(make_int2(L.rows[2 * r] + ib, L.rows[2 * r + 1]));
@@ -208,6 +215,9 @@ int upload_tables(tds_sim* s) {
     if ((rc = dalloc(s, &s->ivals, ivals.size() * sizeof(int4)))) return rc;
     CK(cudaMemcpy(s->rows, rows.data(), rows.size() * sizeof(int2), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(s->ivals, ivals.data(), ivals.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    if (desc.empty()) desc.assign(4, 0u);
+    if ((rc = dalloc(s, &s->desc, desc.size() * sizeof(uint32_t)))) return rc;
+    CK(cudaMemcpy(s->desc, desc.data(), desc.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
 
     // replica table: parameters, fixed-point scales, cell level and bucket range
     std::vector<RepParams<real>> rp(s->R);
@@ -243,6 +253,7 @@ int upload_tables(tds_sim* s) {
         q.C = lv.L.C;
         q.gx = lv.L.gx, q.gy = lv.L.gy, q.gz = lv.L.gz;
         q.row_off = row_off[s->level_of[r]];
+        q.desc_off = desc_off[s->level_of[r]];
         q.n = s->n_rep[r];
         q.off = s->off[r];
         base += (long long)lv.L.C + 1;  // + the bucket of particles off the surface cells
@@ -386,6 +397,8 @@ void launch_one_step(tds_sim* s, const real* noise) {
     a.cnt_o = s->cnt[o];
     a.key_o = s->key[o];
     a.rank_o = s->rank[o];
+    a.key_in = s->key[c];
+    a.desc = s->desc;
     a.perm = s->perm;
     a.start = s->start;
     a.count = s->count;

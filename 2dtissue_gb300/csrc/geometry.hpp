@@ -51,6 +51,11 @@ struct CellLevel {
 // origin: grid corner (mesh bounding box minus a margin of >= 2 cells).
 void build_cell_level(const Mesh& m, double h, const double origin[3], CellLevel& L);
 
+// Per surface cell, the ids of its 27 neighbour cells as 9 x-runs (rows dy, dz in -1..1, in the
+// order r = (dz + 1) * 3 + (dy + 1)); entry = id of the run's first cell << 4 | (x offset of that
+// cell from ix - 1) << 2 | number of cells in the run (0..3). 12 words per cell (3 spare).
+void build_cell_descriptors(const CellLevel& L, std::vector<uint32_t>& desc);
+
 // Seeded placement: face picked with probability proportional to its 3D area, uniform
 // barycentric position, polarity angle uniform in [0, 2pi) in the face frame
 // (e1 = normalize(B - A), e2 = n x e1), expressed as a chart angle.

@@ -66,7 +66,8 @@ struct RepParams {
     double inv_n;                         // 1 / particles in this replica
     int force_mode, base, C, gx;          // bucket base, surface cells, grid size
     int gy, gz, row_off, n;               // row table offset of the level
-    int off, pad3, pad4, pad5;            // off: global index of the replica's first particle
+    int off, desc_off, pad4, pad5;        // off: global index of the replica's first particle;
+                                          // desc_off: the level's descriptor offset (uint4 units)
 };
 
 template <typename real>
@@ -83,6 +84,8 @@ struct StepArgs {
     int* cnt_o;
     int* key_o;
     int* rank_o;
+    const int* key_in;  // cell bucket of each particle (physical order)
+    const uint4* desc;  // per-cell neighbour-run descriptors, all levels
     const int* perm;
     const int* start;
     int* count;
@@ -227,8 +230,10 @@ __device__ int locate(const real* rec, const int4* adj, int G, const int* bs, co
 // seam wrap on the unit-square chart (gluing maps of EuclideanTiling::processPoints,
 // EuclideanTiling.cpp:112-154); first side crossed along the segment; bounded.
 // ---------------------------------------------------------------------------------------------
+// The chart vectors (vx, vy) (velocity) and (wx, wy) (polarity direction) are rotated with the
+// gluing map's linear part; the polarity angle is atan2(wy, wx) afterwards.
 template <typename real>
-__device__ int seam_wrap(real sx, real sy, real& ex, real& ey, real& th, real& vx, real& vy, int& nw) {
+__device__ int seam_wrap(real sx, real sy, real& ex, real& ey, real& vx, real& vy, real& wx, real& wy, int& nw) {
     int excl = -1;
     int w = 0;
     const real one = (real)1, zero = (real)0;
@@ -279,14 +284,16 @@ __device__ int seam_wrap(real sx, real sy, real& ex, real& ey, real& th, real& v
             nx = -ey, ny = ex;
         }
         ex = nx, ey = ny;
-        if (best <= 1) {
+        if (best <= 1) {  // rotation by -90 degrees
             vnx = vy, vny = -vx;
-            th = th - kPi<real>() * (real)0.5;
-        } else {
+            vx = vnx, vy = vny;
+            vnx = wy, vny = -wx;
+        } else {  // rotation by +90 degrees
             vnx = -vy, vny = vx;
-            th = th + kPi<real>() * (real)0.5;
+            vx = vnx, vy = vny;
+            vnx = -wy, vny = wx;
         }
-        vx = vnx, vy = vny;
+        wx = vnx, wy = vny;
         excl = (best == 0) ? 3 : (best == 1) ? 2 : (best == 2) ? 1 : 0;
     }
     nw = w;
@@ -298,13 +305,6 @@ __device__ int seam_wrap(real sx, real sy, real& ex, real& ey, real& th, real& v
     return 0;
 }
 
-template <typename real>
-__device__ __forceinline__ real norm_angle(real th) {
-    const real pi = kPi<real>(), twopi = (real)2 * kPi<real>();
-    if (th > pi || th <= -pi) th = th - twopi * d_floor((th + pi) / twopi);
-    if (th <= -pi) th += twopi;
-    return th;
-}
 
 // ---------------------------------------------------------------------------------------------
 // compact surface-cell list
@@ -344,15 +344,61 @@ __device__ __forceinline__ void add_tile(int* tile_sum, int key) {
 }
 
 // ---------------------------------------------------------------------------------------------
+// order-parameter partial sums
+// ---------------------------------------------------------------------------------------------
+// FP32 build: per-particle terms in [-1, 1] are rounded to 25-bit fixed point, so that a warp
+// sum fits 32 bits and is one instruction; FP64 build: 64-bit fixed point (2^phiscale).
+template <typename real>
+struct PhiPart;
+template <>
+struct PhiPart<float> {
+    static constexpr float kScale = 33554432.0f;  // 2^25
+    int v[6];
+    __device__ void zero() {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) v[k] = 0;
+    }
+    __device__ void set(int k, float x, double) { v[k] = __float2int_rn(x * kScale); }
+    __device__ void warp_sum(unsigned mask) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) v[k] = __reduce_add_sync(mask, v[k]);
+    }
+    __device__ long long to_acc(int k, double phiscale) const {
+        // rescale to the replica's 64-bit accumulator unit
+        return (long long)v[k] * (long long)(phiscale / (double)kScale);
+    }
+};
+template <>
+struct PhiPart<double> {
+    long long v[6];
+    __device__ void zero() {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) v[k] = 0;
+    }
+    __device__ void set(int k, double x, double phiscale) { v[k] = __double2ll_rn(x * phiscale); }
+    __device__ void warp_sum(unsigned mask) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            long long x = v[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(mask, x, o);
+            v[k] = x;
+        }
+    }
+    __device__ long long to_acc(int k, double) const { return v[k]; }
+};
+
+// ---------------------------------------------------------------------------------------------
 // k_step
 // ---------------------------------------------------------------------------------------------
 template <typename real>
-__global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs<real> a) {
+__global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a) {
     typedef R4<real> r4;
     const int q = blockIdx.x * kStepThreads + threadIdx.x;
     const bool active = q < a.N;
     int rep = -1;
-    long long ph[6] = {0, 0, 0, 0, 0, 0};
+    PhiPart<real> ph;
+    ph.zero();
     int st = 0;
     const long long step = *a.d_step;
     if (active) {
@@ -361,6 +407,7 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs<real> a
         const r4 PL = a.pol[s];
         const R2<real> U = a.uv[s];
         const int id = a.ids[s];
+        const int key0 = a.key_in[s];
         const int f = real_to_face(PL.w);
         rep = (int)((unsigned)id >> a.local_bits);
         const unsigned local = (unsigned)id & ((1u << a.local_bits) - 1u);
@@ -369,56 +416,60 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs<real> a
         const real px = PL.x, py = PL.y, pz = PL.z;
         const real r_max2 = rp.r_max2, twoR = rp.twoR;
 
-        // candidate ranges: 9 rows (dy, dz) x 3 consecutive cells in x
-        int ix, iy, iz;
-        cell_coords(rp, P.x, P.y, P.z, ix, iy, iz);
-        int t0[9], t1[9];
+        // candidate ranges: the 9 x-runs of the particle's cell (static descriptors); ranges are
+        // packed as (start, count) to run one flat loop over all candidates
+        int rs[9], rc[9];
+        int total = 0;
+        const int id0 = key0 - rp.base;
+        if (id0 < rp.C) {
+            const uint4* dp = a.desc + (size_t)rp.desc_off + (size_t)id0 * 3;
+            const uint4 d0 = dp[0], d1 = dp[1], d2 = dp[2];
+            const unsigned e[9] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w, d2.x};
 #pragma unroll
-        for (int r = 0; r < 9; ++r) {
-            const int2 R = a.rows[rp.row_off + (iz + r / 3 - 1) * rp.gy + (iy + r % 3 - 1)];
-            int ida = 0x7fffffff, idb = -1;
-            for (int k = 0; k < R.y; ++k) {
-                const int4 I = a.ivals[R.x + k];
-                const int lo = max(I.x, ix - 1), hi = min(I.y, ix + 1);
-                if (lo <= hi) {
-                    ida = min(ida, I.z + lo - I.x);
-                    idb = max(idb, I.z + hi - I.x);
-                }
+            for (int r = 0; r < 9; ++r) {
+                const int first = (int)(e[r] >> 4), len = (int)(e[r] & 3u);
+                const int b0 = rp.base + first;
+                const int t0 = len ? a.start[b0] : 0;
+                const int t1 = len ? a.start[b0 + len] : 0;
+                rs[r] = t0;
+                rc[r] = t1 - t0;
+                total += t1 - t0;
             }
-            if (ida <= idb) {
-                t0[r] = a.start[rp.base + ida];
-                t1[r] = a.start[rp.base + idb + 1];
-            } else {
-                t0[r] = 0, t1[r] = 0;
-            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < 9; ++r) rs[r] = 0, rc[r] = 0;
         }
         // pair sums (fixed point: the sum is independent of the neighbour order)
         long long Fx = 0, Fy = 0, Fz = 0, Mx = 0, My = 0, Mz = 0;
         int cnt = 0;
         const real pscale = (real)kPolScale;
-#pragma unroll 1
-        for (int r = 0; r < 9; ++r) {
-#pragma unroll 2
-            for (int t = t0[r]; t < t1[r]; ++t) {
-                const int j = a.perm[t];
-                const r4 Q = a.pos[j];
-                const real dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
-                const real d2 = dx * dx + dy * dy + dz * dz;
-                if (d2 < r_max2 && j != s) {
-                    const r4 QL = a.pol[j];
-                    const real d = d_sqrt(d2);
-                    const real fm = d < twoR ? rp.k * (twoR - d) * rp.inv_twoR : -(rp.adh_scale * (d - twoR));
-                    if (d > (real)0) {
-                        const real c = fm / d;
-                        Fx += to_fix(c * dx, rp.fscale);
-                        Fy += to_fix(c * dy, rp.fscale);
-                        Fz += to_fix(c * dz, rp.fscale);
-                    }
-                    Mx += to_fix(QL.x, pscale);
-                    My += to_fix(QL.y, pscale);
-                    Mz += to_fix(QL.z, pscale);
-                    ++cnt;
+        int r = 0, t = rs[0], left = rc[0];
+        for (int k = 0; k < total; ++k) {
+            while (left == 0) {
+                ++r;
+                t = rs[r];
+                left = rc[r];
+            }
+            const int j = a.perm[t];
+            ++t;
+            --left;
+            const r4 Q = a.pos[j];
+            const real dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
+            const real d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 < r_max2 && j != s) {
+                const r4 QL = a.pol[j];
+                const real d = d_sqrt(d2);
+                const real fm = d < twoR ? rp.k * (twoR - d) * rp.inv_twoR : -(rp.adh_scale * (d - twoR));
+                if (d > (real)0) {
+                    const real c = fm / d;
+                    Fx += to_fix(c * dx, rp.fscale);
+                    Fy += to_fix(c * dy, rp.fscale);
+                    Fz += to_fix(c * dz, rp.fscale);
                 }
+                Mx += to_fix(QL.x, pscale);
+                My += to_fix(QL.y, pscale);
+                Mz += to_fix(QL.z, pscale);
+                ++cnt;
             }
         }
         if (cnt >= kNbrMax) st |= ST_NBR;
@@ -428,7 +479,8 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs<real> a
         const real mxr = from_fix(Mx, ips), myr = from_fix(My, ips), mzr = from_fix(Mz, ips);
 
         // tangent projection and velocity
-        const real nx = g[12], ny = g[13], nz = g[14];
+        const r4 gn = *reinterpret_cast<const r4*>(g + 12);  // n, pad
+        const real nx = gn.x, ny = gn.y, nz = gn.z;
         const real Fn = Fxr * nx + Fyr * ny + Fzr * nz;
         const real Tx = Fxr - Fn * nx, Ty = Fyr - Fn * ny, Tz = Fzr - Fn * nz;
         real vx, vy, vz;
@@ -462,16 +514,15 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs<real> a
         d_sincos(delta, &sd, &cd);
         const real npx = ny * pz - nz * py, npy = nz * px - nx * pz, npz = nx * py - ny * px;
         const real p2x = cd * px + sd * npx, p2y = cd * py + sd * npy, p2z = cd * pz + sd * npz;
-        const real w0 = g[6] * p2x + g[7] * p2y + g[8] * p2z;
-        const real w1 = g[9] * p2x + g[10] * p2y + g[11] * p2z;
-        real th = d_atan2(w1, w0);
-        // chart advance with the face's affine map, then seam wrap
+        // chart direction of the new polarity and chart velocity through the face's map
+        real w0 = g[6] * p2x + g[7] * p2y + g[8] * p2z;
+        real w1 = g[9] * p2x + g[10] * p2y + g[11] * p2z;
         real vu = g[6] * vx + g[7] * vy + g[8] * vz;
         real vv = g[9] * vx + g[10] * vy + g[11] * vz;
         real u2 = U.x + rp.dt * vu, v2 = U.y + rp.dt * vv;
         int nw = 0;
-        if (seam_wrap(U.x, U.y, u2, v2, th, vu, vv, nw)) st |= ST_WRAP;
-        th = norm_angle(th);
+        if (seam_wrap(U.x, U.y, u2, v2, vu, vv, w0, w1, nw)) st |= ST_WRAP;
+        const real th = d_atan2(w1, w0);
         int mode = 0;
         const int f2 = locate(a.rec, a.adj, a.G, a.bin_start, a.bin_faces, u2, v2, f, mode);
         if (mode == 2) st |= ST_LOCATE;
@@ -480,8 +531,13 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs<real> a
         const real rx = h[24] + h[0] * du + h[3] * dv;
         const real ry = h[25] + h[1] * du + h[4] * dv;
         const real rz = h[26] + h[2] * du + h[5] * dv;
+        // new 3D polarity: normalize(J_f2 w) (= normalize(J_f2 (cos th, sin th)))
         real qx, qy, qz;
-        polarity3(h, th, qx, qy, qz);
+        {
+            const real ex = h[0] * w0 + h[3] * w1, ey = h[1] * w0 + h[4] * w1, ez = h[2] * w0 + h[5] * w1;
+            const real en = d_sqrt(ex * ex + ey * ey + ez * ez);
+            qx = ex / en, qy = ey / en, qz = ez / en;
+        }
         if (!(is_finite(rx) && is_finite(ry) && is_finite(rz) && is_finite(u2) && is_finite(v2) && is_finite(th)))
             st |= ST_NONFINITE;
 
@@ -511,12 +567,11 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs<real> a
         const real ax = rx - a.cx, ay = ry - a.cy, az = rz - a.cz;
         const real Lx = ay * vz - az * vy, Ly = az * vx - ax * vz, Lz = ax * vy - ay * vx;
         const real Ln = d_sqrt(Lx * Lx + Ly * Ly + Lz * Lz);
-        const real ps = (real)rp.phiscale;
         if (Ln > (real)0) {
-            ph[0] = to_fix(Lx / Ln, ps), ph[1] = to_fix(Ly / Ln, ps), ph[2] = to_fix(Lz / Ln, ps);
+            ph.set(0, Lx / Ln, rp.phiscale), ph.set(1, Ly / Ln, rp.phiscale), ph.set(2, Lz / Ln, rp.phiscale);
         }
         if (vn > (real)0) {
-            ph[3] = to_fix(vx / vn, ps), ph[4] = to_fix(vy / vn, ps), ph[5] = to_fix(vz / vn, ps);
+            ph.set(3, vx / vn, rp.phiscale), ph.set(4, vy / vn, rp.phiscale), ph.set(5, vz / vn, rp.phiscale);
         }
     }
     if (st) atomicOr(a.status, st);
@@ -531,24 +586,21 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs<real> a
     if (amask) rep0 = __shfl_sync(FULL, rep, __ffs(amask) - 1);
     const bool same = __all_sync(FULL, !active || rep == rep0);
     const int copy = blockIdx.x % kPhiCopies;
+    const double phis = rep0 >= 0 ? a.reps[rep0].phiscale : 1.0;
     if (same) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            long long v = ph[k];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
-            ph[k] = v;
-        }
+        ph.warp_sum(FULL);
         if (lane == 0) {
             s_rep[warp] = rep0;
 #pragma unroll
-            for (int k = 0; k < 6; ++k) s_ph[warp][k] = ph[k];
+            for (int k = 0; k < 6; ++k) s_ph[warp][k] = ph.to_acc(k, phis);
         }
     } else {
         if (active) {
+            const double myphis = a.reps[rep].phiscale;
 #pragma unroll
             for (int k = 0; k < 6; ++k)
-                atomicAdd(&a.phi_acc[((size_t)rep * kPhiCopies + copy) * 6 + k], (unsigned long long)ph[k]);
+                atomicAdd(&a.phi_acc[((size_t)rep * kPhiCopies + copy) * 6 + k],
+                          (unsigned long long)ph.to_acc(k, myphis));
         }
         if (lane == 0) s_rep[warp] = -1;
     }
@@ -558,14 +610,14 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs<real> a
         int cur = -1;
         long long acc = 0;
         for (int w = 0; w <= kStepThreads / 32; ++w) {
-            const int r = (w < kStepThreads / 32) ? s_rep[w] : -2;
-            if (r != cur) {
+            const int rr = (w < kStepThreads / 32) ? s_rep[w] : -2;
+            if (rr != cur) {
                 if (cur >= 0)
                     atomicAdd(&a.phi_acc[((size_t)cur * kPhiCopies + copy) * 6 + k], (unsigned long long)acc);
-                cur = r;
+                cur = rr;
                 acc = 0;
             }
-            if (r >= 0) acc += s_ph[w][k];
+            if (rr >= 0) acc += s_ph[w][k];
         }
     }
 }
@@ -784,12 +836,13 @@ __global__ void k_debug_wrap(int n, const double* uv_old, double* uv, double* th
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     real ex = (real)uv[2 * i], ey = (real)uv[2 * i + 1];
-    real t = th ? (real)th[i] : (real)0;
+    real wx = (real)1, wy = (real)0;
+    if (th) d_sincos((real)th[i], &wy, &wx);
     real vx = vel ? (real)vel[2 * i] : (real)0, vy = vel ? (real)vel[2 * i + 1] : (real)0;
     int nw = 0;
-    seam_wrap((real)uv_old[2 * i], (real)uv_old[2 * i + 1], ex, ey, t, vx, vy, nw);
+    seam_wrap((real)uv_old[2 * i], (real)uv_old[2 * i + 1], ex, ey, vx, vy, wx, wy, nw);
     uv[2 * i] = ex, uv[2 * i + 1] = ey;
-    if (th) th[i] = t;
+    if (th) th[i] = d_atan2(wy, wx);
     if (vel) vel[2 * i] = vx, vel[2 * i + 1] = vy;
     if (nw_out) nw_out[i] = nw;
 }
