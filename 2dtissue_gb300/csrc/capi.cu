@@ -240,12 +240,19 @@ int upload_tables(tds_sim* s) {
         q.eta = (real)p.eta;
         q.dt = (real)p.dt;
         q.inv_h = (real)(1.0 / h);
+        // Fixed-point scales of the pair sums. A force term is bounded by B = max(k, k_adh) and a
+        // polarity term by 1. FP32: terms below 2^21 (rounded exactly by the magic-add), at most
+        // 256 terms in an int32. FP64: terms below 2^52, at most 1024 terms in an int64.
         const double B = std::max({p.k_rep, p.k_adh, 1e-30});
-        int S = (int)std::floor(52.0 - std::log2(B));
-        S = std::max(0, std::min(S, 60));
+        const bool fp32 = sizeof(real) == 4;
+        int S = (int)std::floor((fp32 ? 21.0 : 52.0) - std::log2(B));
+        S = std::max(-60, std::min(S, 60));
         q.fscale = (real)std::ldexp(1.0, S);
         q.inv_fscale = (real)std::ldexp(1.0, -S);
+        q.pscale = (real)std::ldexp(1.0, fp32 ? 20 : 50);
+        q.inv_pscale = (real)std::ldexp(1.0, fp32 ? -20 : -50);
         q.phiscale = std::ldexp(1.0, 62 - ceil_log2((long long)s->n_rep[r] + 1));
+        q.phi_ratio = (long long)std::ldexp(1.0, 62 - ceil_log2((long long)s->n_rep[r] + 1) - 21);
         q.inv_n = 1.0 / std::max(1, s->n_rep[r]);
         q.force_mode = p.force_mode;
         q.ox = (real)lv.origin[0], q.oy = (real)lv.origin[1], q.oz = (real)lv.origin[2];

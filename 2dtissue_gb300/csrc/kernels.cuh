@@ -37,13 +37,13 @@ enum : int {
 
 constexpr int kRec = 32;          // reals per face record
 constexpr int kMaxWraps = 8;      // seam wraps per particle per step
-constexpr int kNbrMax = 1024;     // neighbours covered by the fixed-point range
+constexpr int kNbrMax32 = 256;    // FP32: neighbours covered by the int32 fixed-point range
+constexpr int kNbrMax64 = 1024;   // FP64: neighbours covered by the int64 fixed-point range
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 32;
 constexpr int kScanTile = kScanThreads * kScanItems;  // buckets per scan tile
 constexpr int kStepThreads = 256;
-constexpr int kPhiCopies = 16;    // spread the order-parameter atomics over copies
-constexpr double kPolScale = 1125899906842624.0;  // 2^50: fixed point of neighbour polarity sums
+constexpr int kPhiCopies = 32;    // spread the order-parameter atomics over copies
 
 template <typename real>
 struct alignas(4 * sizeof(real)) R4 {
@@ -61,9 +61,10 @@ struct RepParams {
     real r_max2, v0, mu, inv_tau;
     real align, eta, dt, inv_h;
     real fscale, inv_fscale, ox, oy;      // force fixed point 2^S, 2^-S; cell-grid origin
-    real oz, pad0, pad1, pad2;
+    real oz, pscale, inv_pscale, pad0;    // neighbour-polarity fixed point
     double phiscale;                      // order-parameter fixed point
     double inv_n;                         // 1 / particles in this replica
+    long long phi_ratio;                  // phiscale / 2^21 (FP32 warp partials -> accumulator)
     int force_mode, base, C, gx;          // bucket base, surface cells, grid size
     int gy, gz, row_off, n;               // row table offset of the level
     int off, desc_off, pad4, pad5;        // off: global index of the replica's first particle;
@@ -124,10 +125,34 @@ __device__ __forceinline__ float d_fma(float a, float b, float c) { return __fma
 __device__ __forceinline__ double d_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float d_mul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double d_mul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ long long to_fix(float x, float s) { return __float2ll_rn(x * s); }
-__device__ __forceinline__ long long to_fix(double x, double s) { return __double2ll_rn(x * s); }
-__device__ __forceinline__ float from_fix(long long v, float inv) { return __ll2float_rn(v) * inv; }
-__device__ __forceinline__ double from_fix(long long v, double inv) { return __ll2double_rn(v) * inv; }
+__device__ __forceinline__ float d_rsqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double d_rsqrt(double x) { return 1.0 / sqrt(x); }
+// sine/cosine of the small per-step rotation angle (|x| < pi)
+__device__ __forceinline__ void d_sincos_small(float x, float* s, float* c) { __sincosf(x, s, c); }
+__device__ __forceinline__ void d_sincos_small(double x, double* s, double* c) { sincos(x, s, c); }
+
+// Fixed-point pair sums: the sum of rounded terms is exact, so it does not depend on the order
+// in which neighbours are visited. FP32: int32 accumulators, terms rounded with the float
+// magic-add (x + 1.5 * 2^23 rounds x to the nearest integer exactly for |x| < 2^22), which keeps
+// the conversion off the conversion unit and the FP64 pipe. FP64: int64 accumulators.
+template <typename real>
+struct Fix;
+template <>
+struct Fix<float> {
+    typedef int acc;
+    static constexpr int kMaxNbr = kNbrMax32;
+    static __device__ __forceinline__ int conv(float xs) {
+        return __float_as_int(__fadd_rn(xs, 12582912.0f)) - 0x4B400000;
+    }
+    static __device__ __forceinline__ float back(int v, float inv) { return __int2float_rn(v) * inv; }
+};
+template <>
+struct Fix<double> {
+    typedef long long acc;
+    static constexpr int kMaxNbr = kNbrMax64;
+    static __device__ __forceinline__ long long conv(double xs) { return __double2ll_rn(xs); }
+    static __device__ __forceinline__ double back(long long v, double inv) { return __ll2double_rn(v) * inv; }
+};
 __device__ __forceinline__ bool is_finite(float x) { return isfinite(x); }
 __device__ __forceinline__ bool is_finite(double x) { return isfinite(x); }
 __device__ __forceinline__ float face_to_real(int f, float) { return __int_as_float(f); }
@@ -352,21 +377,18 @@ template <typename real>
 struct PhiPart;
 template <>
 struct PhiPart<float> {
-    static constexpr float kScale = 33554432.0f;  // 2^25
     int v[6];
     __device__ void zero() {
 #pragma unroll
         for (int k = 0; k < 6; ++k) v[k] = 0;
     }
-    __device__ void set(int k, float x, double) { v[k] = __float2int_rn(x * kScale); }
+    __device__ void set(int k, float x, double) { v[k] = Fix<float>::conv(x * 2097152.0f); }  // 2^21
     __device__ void warp_sum(unsigned mask) {
 #pragma unroll
         for (int k = 0; k < 6; ++k) v[k] = __reduce_add_sync(mask, v[k]);
     }
-    __device__ long long to_acc(int k, double phiscale) const {
-        // rescale to the replica's 64-bit accumulator unit
-        return (long long)v[k] * (long long)(phiscale / (double)kScale);
-    }
+    // in the replica's 64-bit accumulator unit (phiscale = phi_ratio * 2^21)
+    __device__ long long to_acc(int k, long long ratio) const { return (long long)v[k] * ratio; }
 };
 template <>
 struct PhiPart<double> {
@@ -385,12 +407,37 @@ struct PhiPart<double> {
             v[k] = x;
         }
     }
-    __device__ long long to_acc(int k, double) const { return v[k]; }
+    __device__ long long to_acc(int k, long long) const { return v[k]; }
 };
 
 // ---------------------------------------------------------------------------------------------
 // k_step
 // ---------------------------------------------------------------------------------------------
+// One neighbour candidate: 3D chord distance test, Szabo force and polarity sums.
+template <typename real>
+__device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<real>& P, const R4<real>& Q,
+                                          const R4<real>* __restrict__ pol, int j, bool self,
+                                          typename Fix<real>::acc (&acc)[6], int& cnt) {
+    const real dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
+    const real d2 = dx * dx + dy * dy + dz * dz;
+    if (d2 < rp.r_max2 && !self) {
+        const R4<real> QL = pol[j];
+        const real rd = d_rsqrt(d2);  // 1/d (d2 > 0 unless two particles coincide)
+        const real d = d2 * rd;
+        const real fm = d < rp.twoR ? rp.k * (rp.twoR - d) * rp.inv_twoR : -(rp.adh_scale * (d - rp.twoR));
+        if (d2 > (real)0) {
+            const real c = fm * rd * rp.fscale;
+            acc[0] += Fix<real>::conv(c * dx);
+            acc[1] += Fix<real>::conv(c * dy);
+            acc[2] += Fix<real>::conv(c * dz);
+        }
+        acc[3] += Fix<real>::conv(QL.x * rp.pscale);
+        acc[4] += Fix<real>::conv(QL.y * rp.pscale);
+        acc[5] += Fix<real>::conv(QL.z * rp.pscale);
+        ++cnt;
+    }
+}
+
 template <typename real>
 __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a) {
     typedef R4<real> r4;
@@ -414,10 +461,8 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
         const RepParams<real>& rp = a.reps[rep];
         const real* g = a.rec + (size_t)f * kRec;
         const real px = PL.x, py = PL.y, pz = PL.z;
-        const real r_max2 = rp.r_max2, twoR = rp.twoR;
 
-        // candidate ranges: the 9 x-runs of the particle's cell (static descriptors); ranges are
-        // packed as (start, count) to run one flat loop over all candidates
+        // candidate ranges: the 9 x-runs of the particle's cell (static descriptors)
         int rs[9], rc[9];
         int total = 0;
         const int id0 = key0 - rp.base;
@@ -439,68 +484,63 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
 #pragma unroll
             for (int r = 0; r < 9; ++r) rs[r] = 0, rc[r] = 0;
         }
-        // pair sums (fixed point: the sum is independent of the neighbour order)
-        long long Fx = 0, Fy = 0, Fz = 0, Mx = 0, My = 0, Mz = 0;
+        // pair sums over all candidates, two per iteration
+        typename Fix<real>::acc acc[6] = {0, 0, 0, 0, 0, 0};
         int cnt = 0;
-        const real pscale = (real)kPolScale;
         int r = 0, t = rs[0], left = rc[0];
-        for (int k = 0; k < total; ++k) {
+        for (int k = 0; k < total; k += 2) {
             while (left == 0) {
                 ++r;
                 t = rs[r];
                 left = rc[r];
             }
-            const int j = a.perm[t];
-            ++t;
+            const int ta = t++;
             --left;
-            const r4 Q = a.pos[j];
-            const real dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
-            const real d2 = dx * dx + dy * dy + dz * dz;
-            if (d2 < r_max2 && j != s) {
-                const r4 QL = a.pol[j];
-                const real d = d_sqrt(d2);
-                const real fm = d < twoR ? rp.k * (twoR - d) * rp.inv_twoR : -(rp.adh_scale * (d - twoR));
-                if (d > (real)0) {
-                    const real c = fm / d;
-                    Fx += to_fix(c * dx, rp.fscale);
-                    Fy += to_fix(c * dy, rp.fscale);
-                    Fz += to_fix(c * dz, rp.fscale);
+            int tb = -1;
+            if (k + 1 < total) {
+                while (left == 0) {
+                    ++r;
+                    t = rs[r];
+                    left = rc[r];
                 }
-                Mx += to_fix(QL.x, pscale);
-                My += to_fix(QL.y, pscale);
-                Mz += to_fix(QL.z, pscale);
-                ++cnt;
+                tb = t++;
+                --left;
             }
+            const int ja = a.perm[ta];
+            const int jb = tb >= 0 ? a.perm[tb] : ja;
+            const r4 Qa = a.pos[ja];
+            const r4 Qb = a.pos[jb];
+            pair_term(rp, P, Qa, a.pol, ja, ja == s, acc, cnt);
+            if (tb >= 0) pair_term(rp, P, Qb, a.pol, jb, jb == s, acc, cnt);
         }
-        if (cnt >= kNbrMax) st |= ST_NBR;
-        const real Fxr = from_fix(Fx, rp.inv_fscale), Fyr = from_fix(Fy, rp.inv_fscale),
-                   Fzr = from_fix(Fz, rp.inv_fscale);
-        const real ips = (real)(1.0 / kPolScale);
-        const real mxr = from_fix(Mx, ips), myr = from_fix(My, ips), mzr = from_fix(Mz, ips);
+        if (cnt >= Fix<real>::kMaxNbr) st |= ST_NBR;
+        const real Fxr = Fix<real>::back(acc[0], rp.inv_fscale), Fyr = Fix<real>::back(acc[1], rp.inv_fscale),
+                   Fzr = Fix<real>::back(acc[2], rp.inv_fscale);
+        const real mxr = Fix<real>::back(acc[3], rp.inv_pscale), myr = Fix<real>::back(acc[4], rp.inv_pscale),
+                   mzr = Fix<real>::back(acc[5], rp.inv_pscale);
 
         // tangent projection and velocity
-        const r4 gn = *reinterpret_cast<const r4*>(g + 12);  // n, pad
-        const real nx = gn.x, ny = gn.y, nz = gn.z;
+        const real nx = g[12], ny = g[13], nz = g[14];
         const real Fn = Fxr * nx + Fyr * ny + Fzr * nz;
         const real Tx = Fxr - Fn * nx, Ty = Fyr - Fn * ny, Tz = Fzr - Fn * nz;
         real vx, vy, vz;
         if (rp.force_mode == 0) {
             vx = rp.v0 * px + rp.mu * Tx, vy = rp.v0 * py + rp.mu * Ty, vz = rp.v0 * pz + rp.mu * Tz;
         } else {
-            const real sp = rp.v0 + d_sqrt(Tx * Tx + Ty * Ty + Tz * Tz);
+            const real t2 = Tx * Tx + Ty * Ty + Tz * Tz;
+            const real sp = rp.v0 + (t2 > (real)0 ? t2 * d_rsqrt(t2) : (real)0);
             vx = sp * px, vy = sp * py, vz = sp * pz;
         }
         // polarity rotation about n: relaxation towards v, alignment with neighbours, noise
-        const real vn = d_sqrt(vx * vx + vy * vy + vz * vz);
-        const real mn = d_sqrt(mxr * mxr + myr * myr + mzr * mzr);
-        real omega = (real)0;
-        if (vn > (real)0) {
+        const real vn2 = vx * vx + vy * vy + vz * vz;
+        const real mn2 = mxr * mxr + myr * myr + mzr * mzr;
+        const real ivn = vn2 > (real)0 ? d_rsqrt(vn2) : (real)0;
+        const real imn = mn2 > (real)0 ? d_rsqrt(mn2) : (real)0;
+        real omega;
+        {
             const real cx = py * vz - pz * vy, cy = pz * vx - px * vz, cz = px * vy - py * vx;
-            omega += (cx * nx + cy * ny + cz * nz) / vn * rp.inv_tau;
-        }
-        if (mn > (real)0) {
-            const real cx = py * mzr - pz * myr, cy = pz * mxr - px * mzr, cz = px * myr - py * mxr;
-            omega += rp.align * (cx * nx + cy * ny + cz * nz) / mn;
+            const real ex = py * mzr - pz * myr, ey = pz * mxr - px * mzr, ez = px * myr - py * mxr;
+            omega = (cx * nx + cy * ny + cz * nz) * ivn * rp.inv_tau + rp.align * (ex * nx + ey * ny + ez * nz) * imn;
         }
         real xi;
         if (a.noise) {
@@ -511,7 +551,7 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
         }
         const real delta = rp.dt * omega + xi;
         real sd, cd;
-        d_sincos(delta, &sd, &cd);
+        d_sincos_small(delta, &sd, &cd);
         const real npx = ny * pz - nz * py, npy = nz * px - nx * pz, npz = nx * py - ny * px;
         const real p2x = cd * px + sd * npx, p2y = cd * py + sd * npy, p2z = cd * pz + sd * npz;
         // chart direction of the new polarity and chart velocity through the face's map
@@ -535,8 +575,8 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
         real qx, qy, qz;
         {
             const real ex = h[0] * w0 + h[3] * w1, ey = h[1] * w0 + h[4] * w1, ez = h[2] * w0 + h[5] * w1;
-            const real en = d_sqrt(ex * ex + ey * ey + ez * ez);
-            qx = ex / en, qy = ey / en, qz = ez / en;
+            const real ien = d_rsqrt(ex * ex + ey * ey + ez * ez);
+            qx = ex * ien, qy = ey * ien, qz = ez * ien;
         }
         if (!(is_finite(rx) && is_finite(ry) && is_finite(rz) && is_finite(u2) && is_finite(v2) && is_finite(th)))
             st |= ST_NONFINITE;
@@ -566,59 +606,41 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
         // order-parameter partials: normalize((r' - c) x v), v / |v|
         const real ax = rx - a.cx, ay = ry - a.cy, az = rz - a.cz;
         const real Lx = ay * vz - az * vy, Ly = az * vx - ax * vz, Lz = ax * vy - ay * vx;
-        const real Ln = d_sqrt(Lx * Lx + Ly * Ly + Lz * Lz);
-        if (Ln > (real)0) {
-            ph.set(0, Lx / Ln, rp.phiscale), ph.set(1, Ly / Ln, rp.phiscale), ph.set(2, Lz / Ln, rp.phiscale);
+        const real Ln2 = Lx * Lx + Ly * Ly + Lz * Lz;
+        if (Ln2 > (real)0) {
+            const real iL = d_rsqrt(Ln2);
+            ph.set(0, Lx * iL, rp.phiscale), ph.set(1, Ly * iL, rp.phiscale), ph.set(2, Lz * iL, rp.phiscale);
         }
-        if (vn > (real)0) {
-            ph.set(3, vx / vn, rp.phiscale), ph.set(4, vy / vn, rp.phiscale), ph.set(5, vz / vn, rp.phiscale);
+        if (vn2 > (real)0) {
+            ph.set(3, vx * ivn, rp.phiscale), ph.set(4, vy * ivn, rp.phiscale), ph.set(5, vz * ivn, rp.phiscale);
         }
     }
     if (st) atomicOr(a.status, st);
 
-    // order-parameter reduction: warp (same replica) -> block -> atomics on one of kPhiCopies
-    __shared__ long long s_ph[kStepThreads / 32][6];
-    __shared__ int s_rep[kStepThreads / 32];
+    // order-parameter reduction: warp sum (same replica) -> atomics on one of kPhiCopies slots
     const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
     const unsigned amask = __ballot_sync(FULL, active);
-    int rep0 = -1;
-    if (amask) rep0 = __shfl_sync(FULL, rep, __ffs(amask) - 1);
+    if (!amask) return;
+    const int rep0 = __shfl_sync(FULL, rep, __ffs(amask) - 1);
     const bool same = __all_sync(FULL, !active || rep == rep0);
-    const int copy = blockIdx.x % kPhiCopies;
-    const double phis = rep0 >= 0 ? a.reps[rep0].phiscale : 1.0;
+    const int copy = (q >> 5) % kPhiCopies;
     if (same) {
         ph.warp_sum(FULL);
-        if (lane == 0) {
-            s_rep[warp] = rep0;
-#pragma unroll
-            for (int k = 0; k < 6; ++k) s_ph[warp][k] = ph.to_acc(k, phis);
-        }
-    } else {
-        if (active) {
-            const double myphis = a.reps[rep].phiscale;
+        if (lane < 6) {
+            const RepParams<real>& rp0 = a.reps[rep0];
+            long long v = 0;
 #pragma unroll
             for (int k = 0; k < 6; ++k)
-                atomicAdd(&a.phi_acc[((size_t)rep * kPhiCopies + copy) * 6 + k],
-                          (unsigned long long)ph.to_acc(k, myphis));
+                if (k == lane) v = ph.to_acc(k, rp0.phi_ratio);
+            atomicAdd(&a.phi_acc[((size_t)rep0 * kPhiCopies + copy) * 6 + lane], (unsigned long long)v);
         }
-        if (lane == 0) s_rep[warp] = -1;
-    }
-    __syncthreads();
-    if (threadIdx.x < 6) {
-        const int k = threadIdx.x;
-        int cur = -1;
-        long long acc = 0;
-        for (int w = 0; w <= kStepThreads / 32; ++w) {
-            const int rr = (w < kStepThreads / 32) ? s_rep[w] : -2;
-            if (rr != cur) {
-                if (cur >= 0)
-                    atomicAdd(&a.phi_acc[((size_t)cur * kPhiCopies + copy) * 6 + k], (unsigned long long)acc);
-                cur = rr;
-                acc = 0;
-            }
-            if (rr >= 0) acc += s_ph[w][k];
-        }
+    } else if (active) {
+        const RepParams<real>& rpm = a.reps[rep];
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+            atomicAdd(&a.phi_acc[((size_t)rep * kPhiCopies + copy) * 6 + k],
+                      (unsigned long long)ph.to_acc(k, rpm.phi_ratio));
     }
 }
 
