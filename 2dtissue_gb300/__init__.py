@@ -23,8 +23,7 @@ from . import build as _build
 TDS_OK = 0
 ERRORS = {1: "invalid argument", 2: "CUDA error / no CUDA device", 3: "mesh error", 4: "device status set",
           5: "out of device memory", 6: "size limit"}
-STATUS_BITS = {1: "non-finite", 2: "wrap limit", 4: "locate fallback", 8: "neighbour overflow",
-               16: "cell overflow", 32: "scan timeout"}
+STATUS_BITS = {1: "non-finite", 2: "wrap limit", 4: "locate fallback", 16: "particle outside the surface cells"}
 
 _lib = None
 
@@ -229,11 +228,11 @@ class Simulation:
         self._check(lib().tds_kernel_timing(self.h, int(bool(enable))))
 
     def kernel_times(self):
-        """{name: (total_ms, launches)} for scan, scatter, step, finalize."""
-        ms = np.zeros(4)
-        n = np.zeros(4, np.int64)
+        """{name: (total_ms, launches)} for scan, scatter, order, step, finalize."""
+        ms = np.zeros(5)
+        n = np.zeros(5, np.int64)
         self._check(lib().tds_kernel_times(self.h, ms.ctypes.data, n.ctypes.data))
-        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(("scan", "scatter", "step", "finalize"))}
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(("scan", "scatter", "order", "step", "finalize"))}
 
     def set_state(self, uv, theta, face=None, r3d=None):
         uv = np.ascontiguousarray(uv, np.float64)

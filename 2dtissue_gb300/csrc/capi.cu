@@ -85,6 +85,7 @@ struct tds_sim {
     int* key[2] = {nullptr, nullptr};
     int* rank[2] = {nullptr, nullptr};
     int* perm = nullptr;
+    int* tmp = nullptr;  // scatter output before the per-cell id order
     int* start = nullptr;
     int* count = nullptr;
     unsigned long long* phi_acc = nullptr;
@@ -106,8 +107,8 @@ struct tds_sim {
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
-    double k_ms[4] = {0, 0, 0, 0};
-    long long k_n[4] = {0, 0, 0, 0};
+    double k_ms[5] = {0, 0, 0, 0, 0};
+    long long k_n[5] = {0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -240,19 +241,8 @@ int upload_tables(tds_sim* s) {
         q.eta = (real)p.eta;
         q.dt = (real)p.dt;
         q.inv_h = (real)(1.0 / h);
-        // Fixed-point scales of the pair sums. A force term is bounded by B = max(k, k_adh) and a
-        // polarity term by 1. FP32: terms below 2^21 (rounded exactly by the magic-add), at most
-        // 256 terms in an int32. FP64: terms below 2^52, at most 1024 terms in an int64.
-        const double B = std::max({p.k_rep, p.k_adh, 1e-30});
-        const bool fp32 = sizeof(real) == 4;
-        int S = (int)std::floor((fp32 ? 21.0 : 52.0) - std::log2(B));
-        S = std::max(-60, std::min(S, 60));
-        q.fscale = (real)std::ldexp(1.0, S);
-        q.inv_fscale = (real)std::ldexp(1.0, -S);
-        q.pscale = (real)std::ldexp(1.0, fp32 ? 20 : 50);
-        q.inv_pscale = (real)std::ldexp(1.0, fp32 ? -20 : -50);
+        // order parameter: warp sums (|.| <= 32) in 64-bit fixed point, N_r terms per replica
         q.phiscale = std::ldexp(1.0, 62 - ceil_log2((long long)s->n_rep[r] + 1));
-        q.phi_ratio = (long long)std::ldexp(1.0, 62 - ceil_log2((long long)s->n_rep[r] + 1) - 21);
         q.inv_n = 1.0 / std::max(1, s->n_rep[r]);
         q.force_mode = p.force_mode;
         q.ox = (real)lv.origin[0], q.oy = (real)lv.origin[1], q.oz = (real)lv.origin[2];
@@ -287,6 +277,7 @@ int alloc_state(tds_sim* s) {
         if ((rc = dalloc(s, &s->rank[b], N * sizeof(int)))) return rc;
     }
     if ((rc = dalloc(s, &s->perm, N * sizeof(int)))) return rc;
+    if ((rc = dalloc(s, &s->tmp, N * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->start, (size_t)(s->M + 1) * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->count, (size_t)s->M * sizeof(int)))) return rc;
     s->n_tiles = (int)((s->M + tdsk::kScanTile - 1) / tdsk::kScanTile);
@@ -389,7 +380,11 @@ void launch_one_step(tds_sim* s, const real* noise) {
     const int nb = (s->N + 255) / 256;
     {
         KernelTimer kt(s, 1);
-        tdsk::k_scatter<<<nb, 256, 0, st>>>(s->key[c], s->rank[c], s->start, s->perm, s->N, s->d_step);
+        tdsk::k_scatter<<<nb, 256, 0, st>>>(s->key[c], s->rank[c], s->start, s->tmp, s->N, s->d_step);
+    }
+    {
+        KernelTimer kt(s, 2);
+        tdsk::k_order<<<nb, 256, 0, st>>>(s->tmp, s->key[c], s->ids[c], s->start, s->perm, s->N);
     }
     tdsk::StepArgs<real> a;
     a.pos = (const R4<real>*)s->pos[c];
@@ -429,11 +424,11 @@ void launch_one_step(tds_sim* s, const real* noise) {
     a.N = s->N;
     const int ns = (s->N + tdsk::kStepThreads - 1) / tdsk::kStepThreads;
     {
-        KernelTimer kt(s, 2);
+        KernelTimer kt(s, 3);
         tdsk::k_step<real><<<ns, tdsk::kStepThreads, 0, st>>>(a);
     }
     {
-        KernelTimer kt(s, 3);
+        KernelTimer kt(s, 4);
         tdsk::k_finalize<real><<<s->R, 128, 0, st>>>(
             s->phi_acc, (const RepParams<real>*)s->reps, s->R, s->series, 0, s->series_cap, s->d_step);
     }
@@ -486,8 +481,8 @@ int run_steps(tds_sim* s, int n, const double* noise_host, bool sync = true) {
     CK(cudaStreamSynchronize(s->stream));
     if (st) {
         char buf[160];
-        std::snprintf(buf, sizeof buf, "device status 0x%x after step %lld (1 non-finite, 2 wrap limit, 4 locate "
-                      "fallback, 8 neighbour overflow, 32 scan timeout)", st, s->step);
+        std::snprintf(buf, sizeof buf, "device status 0x%x after step %lld (1 non-finite, 2 wrap limit, 4 locate fallback, "
+                      "16 particle outside the surface cells)", st, s->step);
         return fail(s, TDS_ERR_STATE, buf);
     }
     return TDS_OK;
@@ -726,14 +721,14 @@ int tds_kernel_timing(tds_sim* s, int enable) {
     if (!s) return TDS_ERR_ARG;
     collect_times(s);
     s->timing = enable != 0;
-    for (int k = 0; k < 4; ++k) s->k_ms[k] = 0, s->k_n[k] = 0;
+    for (int k = 0; k < 5; ++k) s->k_ms[k] = 0, s->k_n[k] = 0;
     return TDS_OK;
 }
 
 int tds_kernel_times(tds_sim* s, double* total_ms, long long* launches) {
     if (!s) return TDS_ERR_ARG;
     collect_times(s);
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < 5; ++k) {
         if (total_ms) total_ms[k] = s->k_ms[k];
         if (launches) launches[k] = s->k_n[k];
     }
@@ -808,7 +803,7 @@ int tds_stream(tds_sim* s, void** stream) {
 
 int tds_kernels_per_step(const tds_sim* s, int* n) {
     if (!s || !n) return TDS_ERR_ARG;
-    *n = 4;
+    *n = 5;
     return TDS_OK;
 }
 

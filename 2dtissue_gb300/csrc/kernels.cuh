@@ -1,9 +1,11 @@
 // sm_103a kernels of the per-step particle update.
 //
-// One step is four launches on the handle's stream (captured in a CUDA graph by the host):
+// One step is five launches on the handle's stream (captured in a CUDA graph by the host):
 //   k_scan     exclusive scan of the cell-list counts; block bases from per-tile counts that the
 //              previous step accumulated (no inter-block waiting)
-//   k_scatter  counting-sort scatter: perm[start[key] + rank] = slot
+//   k_scatter  counting-sort scatter: tmp[start[key] + rank] = slot (rank from atomics)
+//   k_order    orders each cell's particles by particle id: the neighbour visiting order, and so
+//              every floating-point sum, is the same on every run
 //   k_step     fused pair sums + tangent projection + polarity update + chart advance + seam
 //              wrap + face location + chart->3D map + next-step cell key/count + order partials
 //   k_finalize order parameter per replica for this step
@@ -31,14 +33,11 @@ enum : int {
     ST_NONFINITE = 1,
     ST_WRAP = 2,
     ST_LOCATE = 4,
-    ST_NBR = 8,
     ST_CELL = 16,
 };
 
 constexpr int kRec = 32;          // reals per face record
 constexpr int kMaxWraps = 8;      // seam wraps per particle per step
-constexpr int kNbrMax32 = 256;    // FP32: neighbours covered by the int32 fixed-point range
-constexpr int kNbrMax64 = 1024;   // FP64: neighbours covered by the int64 fixed-point range
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 32;
 constexpr int kScanTile = kScanThreads * kScanItems;  // buckets per scan tile
@@ -60,11 +59,9 @@ struct RepParams {
     real twoR, inv_twoR, k, adh_scale;  // adh_scale = k_adh / (r_max - 2R)
     real r_max2, v0, mu, inv_tau;
     real align, eta, dt, inv_h;
-    real fscale, inv_fscale, ox, oy;      // force fixed point 2^S, 2^-S; cell-grid origin
-    real oz, pscale, inv_pscale, pad0;    // neighbour-polarity fixed point
-    double phiscale;                      // order-parameter fixed point
+    real ox, oy, oz, pad0;                // cell-grid origin
+    double phiscale;                      // order-parameter fixed point (warp sums -> int64)
     double inv_n;                         // 1 / particles in this replica
-    long long phi_ratio;                  // phiscale / 2^21 (FP32 warp partials -> accumulator)
     int force_mode, base, C, gx;          // bucket base, surface cells, grid size
     int gy, gz, row_off, n;               // row table offset of the level
     int off, desc_off, pad4, pad5;        // off: global index of the replica's first particle;
@@ -127,32 +124,7 @@ __device__ __forceinline__ float d_mul(float a, float b) { return __fmul_rn(a, b
 __device__ __forceinline__ double d_mul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float d_rsqrt(float x) { return rsqrtf(x); }
 __device__ __forceinline__ double d_rsqrt(double x) { return 1.0 / sqrt(x); }
-// sine/cosine of the small per-step rotation angle (|x| < pi)
-__device__ __forceinline__ void d_sincos_small(float x, float* s, float* c) { __sincosf(x, s, c); }
-__device__ __forceinline__ void d_sincos_small(double x, double* s, double* c) { sincos(x, s, c); }
 
-// Fixed-point pair sums: the sum of rounded terms is exact, so it does not depend on the order
-// in which neighbours are visited. FP32: int32 accumulators, terms rounded with the float
-// magic-add (x + 1.5 * 2^23 rounds x to the nearest integer exactly for |x| < 2^22), which keeps
-// the conversion off the conversion unit and the FP64 pipe. FP64: int64 accumulators.
-template <typename real>
-struct Fix;
-template <>
-struct Fix<float> {
-    typedef int acc;
-    static constexpr int kMaxNbr = kNbrMax32;
-    static __device__ __forceinline__ int conv(float xs) {
-        return __float_as_int(__fadd_rn(xs, 12582912.0f)) - 0x4B400000;
-    }
-    static __device__ __forceinline__ float back(int v, float inv) { return __int2float_rn(v) * inv; }
-};
-template <>
-struct Fix<double> {
-    typedef long long acc;
-    static constexpr int kMaxNbr = kNbrMax64;
-    static __device__ __forceinline__ long long conv(double xs) { return __double2ll_rn(xs); }
-    static __device__ __forceinline__ double back(long long v, double inv) { return __ll2double_rn(v) * inv; }
-};
 __device__ __forceinline__ bool is_finite(float x) { return isfinite(x); }
 __device__ __forceinline__ bool is_finite(double x) { return isfinite(x); }
 __device__ __forceinline__ float face_to_real(int f, float) { return __int_as_float(f); }
@@ -369,55 +341,13 @@ __device__ __forceinline__ void add_tile(int* tile_sum, int key) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// order-parameter partial sums
-// ---------------------------------------------------------------------------------------------
-// FP32 build: per-particle terms in [-1, 1] are rounded to 25-bit fixed point, so that a warp
-// sum fits 32 bits and is one instruction; FP64 build: 64-bit fixed point (2^phiscale).
-template <typename real>
-struct PhiPart;
-template <>
-struct PhiPart<float> {
-    int v[6];
-    __device__ void zero() {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) v[k] = 0;
-    }
-    __device__ void set(int k, float x, double) { v[k] = Fix<float>::conv(x * 2097152.0f); }  // 2^21
-    __device__ void warp_sum(unsigned mask) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) v[k] = __reduce_add_sync(mask, v[k]);
-    }
-    // in the replica's 64-bit accumulator unit (phiscale = phi_ratio * 2^21)
-    __device__ long long to_acc(int k, long long ratio) const { return (long long)v[k] * ratio; }
-};
-template <>
-struct PhiPart<double> {
-    long long v[6];
-    __device__ void zero() {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) v[k] = 0;
-    }
-    __device__ void set(int k, double x, double phiscale) { v[k] = __double2ll_rn(x * phiscale); }
-    __device__ void warp_sum(unsigned mask) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            long long x = v[k];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(mask, x, o);
-            v[k] = x;
-        }
-    }
-    __device__ long long to_acc(int k, long long) const { return v[k]; }
-};
-
-// ---------------------------------------------------------------------------------------------
 // k_step
 // ---------------------------------------------------------------------------------------------
 // One neighbour candidate: 3D chord distance test, Szabo force and polarity sums.
 template <typename real>
 __device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<real>& P, const R4<real>& Q,
-                                          const R4<real>* __restrict__ pol, int j, bool self,
-                                          typename Fix<real>::acc (&acc)[6], int& cnt) {
+                                          const R4<real>* __restrict__ pol, int j, bool self, real (&acc)[6],
+                                          int& cnt) {
     const real dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
     const real d2 = dx * dx + dy * dy + dz * dz;
     if (d2 < rp.r_max2 && !self) {
@@ -426,14 +356,14 @@ __device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<re
         const real d = d2 * rd;
         const real fm = d < rp.twoR ? rp.k * (rp.twoR - d) * rp.inv_twoR : -(rp.adh_scale * (d - rp.twoR));
         if (d2 > (real)0) {
-            const real c = fm * rd * rp.fscale;
-            acc[0] += Fix<real>::conv(c * dx);
-            acc[1] += Fix<real>::conv(c * dy);
-            acc[2] += Fix<real>::conv(c * dz);
+            const real c = fm * rd;
+            acc[0] += c * dx;
+            acc[1] += c * dy;
+            acc[2] += c * dz;
         }
-        acc[3] += Fix<real>::conv(QL.x * rp.pscale);
-        acc[4] += Fix<real>::conv(QL.y * rp.pscale);
-        acc[5] += Fix<real>::conv(QL.z * rp.pscale);
+        acc[3] += QL.x;
+        acc[4] += QL.y;
+        acc[5] += QL.z;
         ++cnt;
     }
 }
@@ -444,8 +374,7 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
     const int q = blockIdx.x * kStepThreads + threadIdx.x;
     const bool active = q < a.N;
     int rep = -1;
-    PhiPart<real> ph;
-    ph.zero();
+    real ph[6] = {0, 0, 0, 0, 0, 0};
     int st = 0;
     const long long step = *a.d_step;
     if (active) {
@@ -484,8 +413,8 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
 #pragma unroll
             for (int r = 0; r < 9; ++r) rs[r] = 0, rc[r] = 0;
         }
-        // pair sums over all candidates, two per iteration
-        typename Fix<real>::acc acc[6] = {0, 0, 0, 0, 0, 0};
+        // pair sums over all candidates (in a fixed order), two per iteration
+        real acc[6] = {0, 0, 0, 0, 0, 0};
         int cnt = 0;
         int r = 0, t = rs[0], left = rc[0];
         for (int k = 0; k < total; k += 2) {
@@ -513,11 +442,8 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
             pair_term(rp, P, Qa, a.pol, ja, ja == s, acc, cnt);
             if (tb >= 0) pair_term(rp, P, Qb, a.pol, jb, jb == s, acc, cnt);
         }
-        if (cnt >= Fix<real>::kMaxNbr) st |= ST_NBR;
-        const real Fxr = Fix<real>::back(acc[0], rp.inv_fscale), Fyr = Fix<real>::back(acc[1], rp.inv_fscale),
-                   Fzr = Fix<real>::back(acc[2], rp.inv_fscale);
-        const real mxr = Fix<real>::back(acc[3], rp.inv_pscale), myr = Fix<real>::back(acc[4], rp.inv_pscale),
-                   mzr = Fix<real>::back(acc[5], rp.inv_pscale);
+        const real Fxr = acc[0], Fyr = acc[1], Fzr = acc[2];
+        const real mxr = acc[3], myr = acc[4], mzr = acc[5];
 
         // tangent projection and velocity
         const real nx = g[12], ny = g[13], nz = g[14];
@@ -551,7 +477,7 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
         }
         const real delta = rp.dt * omega + xi;
         real sd, cd;
-        d_sincos_small(delta, &sd, &cd);
+        d_sincos(delta, &sd, &cd);
         const real npx = ny * pz - nz * py, npy = nz * px - nx * pz, npz = nx * py - ny * px;
         const real p2x = cd * px + sd * npx, p2y = cd * py + sd * npy, p2z = cd * pz + sd * npz;
         // chart direction of the new polarity and chart velocity through the face's map
@@ -609,10 +535,10 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
         const real Ln2 = Lx * Lx + Ly * Ly + Lz * Lz;
         if (Ln2 > (real)0) {
             const real iL = d_rsqrt(Ln2);
-            ph.set(0, Lx * iL, rp.phiscale), ph.set(1, Ly * iL, rp.phiscale), ph.set(2, Lz * iL, rp.phiscale);
+            ph[0] = Lx * iL, ph[1] = Ly * iL, ph[2] = Lz * iL;
         }
         if (vn2 > (real)0) {
-            ph.set(3, vx * ivn, rp.phiscale), ph.set(4, vy * ivn, rp.phiscale), ph.set(5, vz * ivn, rp.phiscale);
+            ph[3] = vx * ivn, ph[4] = vy * ivn, ph[5] = vz * ivn;
         }
     }
     if (st) atomicOr(a.status, st);
@@ -626,21 +552,26 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
     const bool same = __all_sync(FULL, !active || rep == rep0);
     const int copy = (q >> 5) % kPhiCopies;
     if (same) {
-        ph.warp_sum(FULL);
-        if (lane < 6) {
-            const RepParams<real>& rp0 = a.reps[rep0];
-            long long v = 0;
+        // fixed butterfly over fixed lanes: the warp sum is the same on every run
 #pragma unroll
-            for (int k = 0; k < 6; ++k)
-                if (k == lane) v = ph.to_acc(k, rp0.phi_ratio);
-            atomicAdd(&a.phi_acc[((size_t)rep0 * kPhiCopies + copy) * 6 + lane], (unsigned long long)v);
+        for (int k = 0; k < 6; ++k) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) ph[k] += __shfl_xor_sync(FULL, ph[k], o);
+        }
+        if (lane < 6) {
+            real v = ph[0];
+#pragma unroll
+            for (int k = 1; k < 6; ++k)
+                if (k == lane) v = ph[k];
+            const long long iv = __double2ll_rn((double)v * a.reps[rep0].phiscale);
+            atomicAdd(&a.phi_acc[((size_t)rep0 * kPhiCopies + copy) * 6 + lane], (unsigned long long)iv);
         }
     } else if (active) {
-        const RepParams<real>& rpm = a.reps[rep];
+        const double ps = a.reps[rep].phiscale;
 #pragma unroll
         for (int k = 0; k < 6; ++k)
             atomicAdd(&a.phi_acc[((size_t)rep * kPhiCopies + copy) * 6 + k],
-                      (unsigned long long)ph.to_acc(k, rpm.phi_ratio));
+                      (unsigned long long)__double2ll_rn((double)ph[k] * ps));
     }
 }
 
@@ -740,6 +671,21 @@ __global__ void k_scatter(const int* __restrict__ key, const int* __restrict__ r
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s == 0) *d_step += 1;
     if (s < N) perm[start[key[s]] + rank[s]] = s;
+}
+
+// Within each cell, particles in increasing particle-id order: perm[start[b] + (number of the
+// cell's particles with a smaller id)] = slot.
+__global__ void k_order(const int* __restrict__ tmp, const int* __restrict__ key, const int* __restrict__ ids,
+                        const int* __restrict__ start, int* __restrict__ perm, int N) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= N) return;
+    const int s = tmp[p];
+    const int b = key[s];
+    const int me = ids[s];
+    const int b0 = start[b], b1 = start[b + 1];
+    int rank = 0;
+    for (int x = b0; x < b1; ++x) rank += ids[tmp[x]] < me;
+    perm[b0 + rank] = s;
 }
 
 // Cell keys, ranks and tile counts of the current state (after start / set_state); counts and

@@ -34,8 +34,8 @@ extern "C" {
 #define TDS_STATUS_NONFINITE 1      /* NaN/Inf in a new position or polarity */
 #define TDS_STATUS_WRAP_LIMIT 2     /* more than 8 seam wraps in one step (position clamped) */
 #define TDS_STATUS_LOCATE_FALLBACK 4 /* no chart face contained the point (nearest face used) */
-#define TDS_STATUS_NBR_OVERFLOW 8   /* >= 1024 neighbours: fixed-point pair sums may overflow */
-#define TDS_STATUS_CELL_OVERFLOW 16 /* a cell-list rank overflowed its field */
+#define TDS_STATUS_RESERVED 8
+#define TDS_STATUS_CELL_OVERFLOW 16 /* a position fell outside the surface-cell list (lost particle) */
 
 typedef struct tds_mesh tds_mesh;
 typedef struct tds_sim tds_sim;
@@ -107,8 +107,8 @@ int tds_num_particles(const tds_sim* sim, int* n_total, int* n_replicas);
  * checked by the next tds_step / tds_get_status. For pipelined callers and device-timed loops. */
 int tds_step_async(tds_sim* sim, int n_steps);
 /* Per-kernel CUDA-event timing of directly launched steps (graphs are not used while enabled).
- * tds_kernel_times returns, per kernel (0 scan, 1 scatter, 2 step, 3 finalize), the summed
- * device time in ms and the launch count since timing was enabled. */
+ * tds_kernel_times returns, per kernel (0 scan, 1 scatter, 2 order, 3 step, 4 finalize), the
+ * summed device time in ms and the launch count since timing was enabled (arrays of 5). */
 int tds_kernel_timing(tds_sim* sim, int enable);
 int tds_kernel_times(tds_sim* sim, double* total_ms, long long* launches);
 /* The CUDA stream every kernel of this handle runs on (cudaStream_t). */
