@@ -144,8 +144,18 @@ void free_graphs(tds_sim* s) {
 template <typename real>
 int upload_tables(tds_sim* s) {
     const tds::FaceTables& t = s->mesh->t;
-    std::vector<real> rec(t.rec.size());
-    for (size_t i = 0; i < rec.size(); ++i) rec[i] = (real)t.rec[i];
+    // device face record (16 reals): chart corners, edge bits, A, J (see kernels.cuh)
+    std::vector<real> rec((size_t)t.F * tdsk::kRec);
+    for (int f = 0; f < t.F; ++f) {
+        const double* h = &t.rec[(size_t)f * tds::kFaceRec];
+        real* d = &rec[(size_t)f * tdsk::kRec];
+        for (int k = 0; k < 6; ++k) d[k] = (real)h[16 + k];
+        d[6] = (real)h[22];
+        d[7] = (real)h[24];
+        for (int k = 0; k < 6; ++k) d[8 + k] = (real)h[k];
+        d[14] = (real)h[25];
+        d[15] = (real)h[26];
+    }
     int rc;
     if ((rc = dalloc(s, (real**)&s->rec, rec.size() * sizeof(real)))) return rc;
     CK(cudaMemcpy(s->rec, rec.data(), rec.size() * sizeof(real), cudaMemcpyHostToDevice));
@@ -368,9 +378,10 @@ void collect_times(tds_sim* s) {
     s->ev_pending.clear();
 }
 
+// Buffer roles: index 0 = step output (and set_state target), index 1 = sorted copy.
 template <typename real>
 void launch_one_step(tds_sim* s, const real* noise) {
-    const int c = s->cur, o = c ^ 1;
+    const int c = 1, o = 0;
     cudaStream_t st = s->stream;
     {
         KernelTimer kt(s, 0);
@@ -380,11 +391,14 @@ void launch_one_step(tds_sim* s, const real* noise) {
     const int nb = (s->N + 255) / 256;
     {
         KernelTimer kt(s, 1);
-        tdsk::k_scatter<<<nb, 256, 0, st>>>(s->key[c], s->rank[c], s->start, s->tmp, s->N, s->d_step);
+        tdsk::k_scatter<<<nb, 256, 0, st>>>(s->key[o], s->rank[o], s->start, s->tmp, s->N, s->d_step);
     }
     {
         KernelTimer kt(s, 2);
-        tdsk::k_order<<<nb, 256, 0, st>>>(s->tmp, s->key[c], s->ids[c], s->start, s->perm, s->N);
+        tdsk::k_order<real><<<nb, 256, 0, st>>>(s->tmp, s->key[o], s->ids[o], s->start, (const R4<real>*)s->pos[o],
+                                                 (const R4<real>*)s->pol[o], (const R2<real>*)s->uv[o],
+                                                 (R4<real>*)s->pos[c], (R4<real>*)s->pol[c], (R2<real>*)s->uv[c],
+                                                 s->ids[c], s->key[c], s->N);
     }
     tdsk::StepArgs<real> a;
     a.pos = (const R4<real>*)s->pos[c];
@@ -401,7 +415,6 @@ void launch_one_step(tds_sim* s, const real* noise) {
     a.rank_o = s->rank[o];
     a.key_in = s->key[c];
     a.desc = s->desc;
-    a.perm = s->perm;
     a.start = s->start;
     a.count = s->count;
     a.tile_sum = s->tile_sum;
@@ -432,7 +445,6 @@ void launch_one_step(tds_sim* s, const real* noise) {
         tdsk::k_finalize<real><<<s->R, 128, 0, st>>>(
             s->phi_acc, (const RepParams<real>*)s->reps, s->R, s->series, 0, s->series_cap, s->d_step);
     }
-    s->cur = o;
 }
 
 template <typename real>

@@ -4,8 +4,10 @@
 //   k_scan     exclusive scan of the cell-list counts; block bases from per-tile counts that the
 //              previous step accumulated (no inter-block waiting)
 //   k_scatter  counting-sort scatter: tmp[start[key] + rank] = slot (rank from atomics)
-//   k_order    orders each cell's particles by particle id: the neighbour visiting order, and so
-//              every floating-point sum, is the same on every run
+//   k_order    orders each cell's particles by particle id (so that the neighbour visiting order,
+//              and every floating-point sum, is the same on every run) and writes the state in
+//              that sorted order: the step kernel reads its own state coalesced and the
+//              candidates of a cell run from consecutive addresses
 //   k_step     fused pair sums + tangent projection + polarity update + chart advance + seam
 //              wrap + face location + chart->3D map + next-step cell key/count + order partials
 //   k_finalize order parameter per replica for this step
@@ -15,12 +17,19 @@
 // CellHelper::get_r3d (CellHelper.cpp:71-160), Validation (Validation.cpp:40-72),
 // count_particle_neighbors (2DTissue.cpp:254-268), calculate_order_parameter (LinearAlgebra.cpp:90-105).
 //
-// State per particle (structure of arrays, in the order of the previous step's cell sort):
+// State per particle (structure of arrays):
 //   pos = (x, y, z, theta)  3D position and chart polarity angle
 //   pol = (px, py, pz, face) unit 3D polarity normalize(J_face (cos theta, sin theta)) and the
 //                            containing chart face (stored with the polarity so that a
 //                            neighbour's polarity is one load)
-//   uv, id
+//   uv, id, key (cell bucket)
+// The step kernel writes the "unsorted" arrays (in the previous cell order); k_order writes the
+// sorted copy (s-prefixed) that the next step kernel reads.
+//
+// Face record (16 reals, 64 bytes in FP32): [0..5] chart corners a, b, c (CCW); [6] canonical
+// edge bits (bit k: edge k evaluated reversed and negated); [7] A.x; [8..13] J = dX/d(uv),
+// column u = [8..10], column v = [11..13]; [14] A.y; [15] A.z (A = 3D image of a). The normal and
+// the pseudo-inverse of J are derived from J where needed.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -36,7 +45,7 @@ enum : int {
     ST_CELL = 16,
 };
 
-constexpr int kRec = 32;          // reals per face record
+constexpr int kRec = 16;          // reals per face record
 constexpr int kMaxWraps = 8;      // seam wraps per particle per step
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 32;
@@ -70,11 +79,11 @@ struct RepParams {
 
 template <typename real>
 struct StepArgs {
-    const R4<real>* pos;
+    const R4<real>* pos;  // state in sorted order (k_order output)
     const R4<real>* pol;
     const R2<real>* uv;
     const int* ids;
-    R4<real>* pos_o;  // outputs in this step's sorted order
+    R4<real>* pos_o;  // outputs, same order
     R4<real>* pol_o;
     R2<real>* uv_o;
     int* ids_o;
@@ -82,9 +91,8 @@ struct StepArgs {
     int* cnt_o;
     int* key_o;
     int* rank_o;
-    const int* key_in;  // cell bucket of each particle (physical order)
+    const int* key_in;  // cell bucket of each particle (sorted order)
     const uint4* desc;  // per-cell neighbour-run descriptors, all levels
-    const int* perm;
     const int* start;
     int* count;
     int* tile_sum;  // [2][n_tiles]
@@ -142,7 +150,7 @@ template <typename real>
 __device__ __forceinline__ void polarity3(const real* g, real th, real& px, real& py, real& pz) {
     real sn, cs;
     d_sincos(th, &sn, &cs);
-    const real qx = g[0] * cs + g[3] * sn, qy = g[1] * cs + g[4] * sn, qz = g[2] * cs + g[5] * sn;
+    const real qx = g[8] * cs + g[11] * sn, qy = g[9] * cs + g[12] * sn, qz = g[10] * cs + g[13] * sn;
     const real qn = d_sqrt(qx * qx + qy * qy + qz * qz);
     px = qx / qn, py = qy / qn, pz = qz / qn;
 }
@@ -156,8 +164,8 @@ __device__ __forceinline__ real orient(real Px, real Py, real Qx, real Qy, real 
 }
 template <typename real>
 __device__ __forceinline__ void edge_values(const real* r, real px, real py, real e[3]) {
-    const int bits = (int)r[22];
-    const real P[3][2] = {{r[16], r[17]}, {r[18], r[19]}, {r[20], r[21]}};
+    const int bits = (int)r[6];
+    const real P[3][2] = {{r[0], r[1]}, {r[2], r[3]}, {r[4], r[5]}};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const int k1 = (k + 1) % 3;
@@ -175,7 +183,37 @@ template <typename real>
 __device__ __forceinline__ real face_score(const real* r, real px, real py) {
     real e[3];
     edge_values(r, px, py, e);
-    return fmin(e[0] * r[28], fmin(e[1] * r[29], e[2] * r[30]));
+    real s = (real)1e30;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int k1 = (k + 1) % 3;
+        const real ex = r[2 * k1] - r[2 * k], ey = r[2 * k1 + 1] - r[2 * k + 1];
+        s = fmin(s, e[k] / d_sqrt(ex * ex + ey * ey));
+    }
+    return s;
+}
+
+// Unit normal and pseudo-inverse Jp = (J^T J)^-1 J^T of a face's chart map.
+template <typename real>
+__device__ __forceinline__ void face_frame(const real* g, real n[3], real Jp[6]) {
+    const real ux = g[8], uy = g[9], uz = g[10], vx = g[11], vy = g[12], vz = g[13];
+    const real cx = uy * vz - uz * vy, cy = uz * vx - ux * vz, cz = ux * vy - uy * vx;
+    const real ic = d_rsqrt(cx * cx + cy * cy + cz * cz);
+    n[0] = cx * ic, n[1] = cy * ic, n[2] = cz * ic;
+    const real g11 = ux * ux + uy * uy + uz * uz, g12 = ux * vx + uy * vy + uz * vz, g22 = vx * vx + vy * vy + vz * vz;
+    const real idet = (real)1 / (g11 * g22 - g12 * g12);
+    const real a11 = g22 * idet, a12 = -g12 * idet, a22 = g11 * idet;
+    Jp[0] = a11 * ux + a12 * vx, Jp[1] = a11 * uy + a12 * vy, Jp[2] = a11 * uz + a12 * vz;
+    Jp[3] = a12 * ux + a22 * vx, Jp[4] = a12 * uy + a22 * vy, Jp[5] = a12 * uz + a22 * vz;
+}
+
+// chart point -> 3D on face record h
+template <typename real>
+__device__ __forceinline__ void face_map(const real* h, real u, real v, real& x, real& y, real& z) {
+    const real du = u - h[0], dv = v - h[1];
+    x = h[7] + h[8] * du + h[11] * dv;
+    y = h[14] + h[9] * du + h[12] * dv;
+    z = h[15] + h[10] * du + h[13] * dv;
 }
 template <typename real>
 __device__ __forceinline__ int bin_coord(real x, int G) {
@@ -378,12 +416,11 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
     int st = 0;
     const long long step = *a.d_step;
     if (active) {
-        const int s = a.perm[q];
-        const r4 P = a.pos[s];
-        const r4 PL = a.pol[s];
-        const R2<real> U = a.uv[s];
-        const int id = a.ids[s];
-        const int key0 = a.key_in[s];
+        const r4 P = a.pos[q];
+        const r4 PL = a.pol[q];
+        const R2<real> U = a.uv[q];
+        const int id = a.ids[q];
+        const int key0 = a.key_in[q];
         const int f = real_to_face(PL.w);
         rep = (int)((unsigned)id >> a.local_bits);
         const unsigned local = (unsigned)id & ((1u << a.local_bits) - 1u);
@@ -435,18 +472,19 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
                 tb = t++;
                 --left;
             }
-            const int ja = a.perm[ta];
-            const int jb = tb >= 0 ? a.perm[tb] : ja;
-            const r4 Qa = a.pos[ja];
-            const r4 Qb = a.pos[jb];
-            pair_term(rp, P, Qa, a.pol, ja, ja == s, acc, cnt);
-            if (tb >= 0) pair_term(rp, P, Qb, a.pol, jb, jb == s, acc, cnt);
+            const int tb2 = tb >= 0 ? tb : ta;
+            const r4 Qa = a.pos[ta];
+            const r4 Qb = a.pos[tb2];
+            pair_term(rp, P, Qa, a.pol, ta, ta == q, acc, cnt);
+            if (tb >= 0) pair_term(rp, P, Qb, a.pol, tb, tb == q, acc, cnt);
         }
         const real Fxr = acc[0], Fyr = acc[1], Fzr = acc[2];
         const real mxr = acc[3], myr = acc[4], mzr = acc[5];
 
         // tangent projection and velocity
-        const real nx = g[12], ny = g[13], nz = g[14];
+        real nrm[3], Jp[6];
+        face_frame(g, nrm, Jp);
+        const real nx = nrm[0], ny = nrm[1], nz = nrm[2];
         const real Fn = Fxr * nx + Fyr * ny + Fzr * nz;
         const real Tx = Fxr - Fn * nx, Ty = Fyr - Fn * ny, Tz = Fzr - Fn * nz;
         real vx, vy, vz;
@@ -481,10 +519,10 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
         const real npx = ny * pz - nz * py, npy = nz * px - nx * pz, npz = nx * py - ny * px;
         const real p2x = cd * px + sd * npx, p2y = cd * py + sd * npy, p2z = cd * pz + sd * npz;
         // chart direction of the new polarity and chart velocity through the face's map
-        real w0 = g[6] * p2x + g[7] * p2y + g[8] * p2z;
-        real w1 = g[9] * p2x + g[10] * p2y + g[11] * p2z;
-        real vu = g[6] * vx + g[7] * vy + g[8] * vz;
-        real vv = g[9] * vx + g[10] * vy + g[11] * vz;
+        real w0 = Jp[0] * p2x + Jp[1] * p2y + Jp[2] * p2z;
+        real w1 = Jp[3] * p2x + Jp[4] * p2y + Jp[5] * p2z;
+        real vu = Jp[0] * vx + Jp[1] * vy + Jp[2] * vz;
+        real vv = Jp[3] * vx + Jp[4] * vy + Jp[5] * vz;
         real u2 = U.x + rp.dt * vu, v2 = U.y + rp.dt * vv;
         int nw = 0;
         if (seam_wrap(U.x, U.y, u2, v2, vu, vv, w0, w1, nw)) st |= ST_WRAP;
@@ -493,14 +531,12 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
         const int f2 = locate(a.rec, a.adj, a.G, a.bin_start, a.bin_faces, u2, v2, f, mode);
         if (mode == 2) st |= ST_LOCATE;
         const real* h = a.rec + (size_t)f2 * kRec;
-        const real du = u2 - h[16], dv = v2 - h[17];
-        const real rx = h[24] + h[0] * du + h[3] * dv;
-        const real ry = h[25] + h[1] * du + h[4] * dv;
-        const real rz = h[26] + h[2] * du + h[5] * dv;
+        real rx, ry, rz;
+        face_map(h, u2, v2, rx, ry, rz);
         // new 3D polarity: normalize(J_f2 w) (= normalize(J_f2 (cos th, sin th)))
         real qx, qy, qz;
         {
-            const real ex = h[0] * w0 + h[3] * w1, ey = h[1] * w0 + h[4] * w1, ez = h[2] * w0 + h[5] * w1;
+            const real ex = h[8] * w0 + h[11] * w1, ey = h[9] * w0 + h[12] * w1, ez = h[10] * w0 + h[13] * w1;
             const real ien = d_rsqrt(ex * ex + ey * ey + ez * ez);
             qx = ex * ien, qy = ey * ien, qz = ez * ien;
         }
@@ -673,10 +709,14 @@ __global__ void k_scatter(const int* __restrict__ key, const int* __restrict__ r
     if (s < N) perm[start[key[s]] + rank[s]] = s;
 }
 
-// Within each cell, particles in increasing particle-id order: perm[start[b] + (number of the
-// cell's particles with a smaller id)] = slot.
+// Within each cell, particles in increasing particle-id order: the particle in slot s goes to
+// start[b] + (number of the cell's particles with a smaller id); its state is copied there.
+template <typename real>
 __global__ void k_order(const int* __restrict__ tmp, const int* __restrict__ key, const int* __restrict__ ids,
-                        const int* __restrict__ start, int* __restrict__ perm, int N) {
+                        const int* __restrict__ start, const R4<real>* __restrict__ pos,
+                        const R4<real>* __restrict__ pol, const R2<real>* __restrict__ uv, R4<real>* __restrict__ spos,
+                        R4<real>* __restrict__ spol, R2<real>* __restrict__ suv, int* __restrict__ sids,
+                        int* __restrict__ skey, int N) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= N) return;
     const int s = tmp[p];
@@ -685,7 +725,12 @@ __global__ void k_order(const int* __restrict__ tmp, const int* __restrict__ key
     const int b0 = start[b], b1 = start[b + 1];
     int rank = 0;
     for (int x = b0; x < b1; ++x) rank += ids[tmp[x]] < me;
-    perm[b0 + rank] = s;
+    const int d = b0 + rank;
+    spos[d] = pos[s];
+    spol[d] = pol[s];
+    suv[d] = uv[s];
+    sids[d] = me;
+    skey[d] = b;
 }
 
 // Cell keys, ranks and tile counts of the current state (after start / set_state); counts and
@@ -714,9 +759,9 @@ __global__ void k_finalize(unsigned long long* phi_acc, const RepParams<real>* r
     __shared__ double s[kPhiCopies * 6];
     const int r = blockIdx.x;
     const int t = threadIdx.x;
-    if (t < kPhiCopies * 6) {
-        unsigned long long* p = &phi_acc[(size_t)r * kPhiCopies * 6 + t];
-        s[t] = (double)(long long)(*p);
+    for (int i = t; i < kPhiCopies * 6; i += blockDim.x) {
+        unsigned long long* p = &phi_acc[(size_t)r * kPhiCopies * 6 + i];
+        s[i] = (double)(long long)(*p);
         *p = 0ull;
     }
     __syncthreads();
@@ -778,10 +823,7 @@ __global__ void k_load_state(const double* i_uv, const double* i_th, const int* 
     if (has_r3d) {
         P.x = (real)i_r3d[3 * i], P.y = (real)i_r3d[3 * i + 1], P.z = (real)i_r3d[3 * i + 2];
     } else {
-        const real du = u - h[16], dv = v - h[17];
-        P.x = h[24] + h[0] * du + h[3] * dv;
-        P.y = h[25] + h[1] * du + h[4] * dv;
-        P.z = h[26] + h[2] * du + h[5] * dv;
+        face_map(h, u, v, P.x, P.y, P.z);
     }
     P.w = (real)i_th[i];
     pos[i] = P;
