@@ -83,12 +83,12 @@ struct tds_sim {
     void* vel[2] = {nullptr, nullptr};
     int* cnt[2] = {nullptr, nullptr};
     int* key[2] = {nullptr, nullptr};
-    int* rank[2] = {nullptr, nullptr};
     int* perm = nullptr;
     int* tmp = nullptr;  // scatter output before the per-cell id order
     int* start = nullptr;
     int* count = nullptr;
     unsigned long long* phi_acc = nullptr;
+    unsigned* done = nullptr;  // warps finished in the current step kernel (fused order parameter)
     double* series = nullptr;
     long long series_cap = 0;  // steps
     int* status = nullptr;
@@ -284,7 +284,6 @@ int alloc_state(tds_sim* s) {
         if ((rc = dalloc(s, (R2<real>**)&s->vel[b], N * sizeof(R2<real>)))) return rc;
         if ((rc = dalloc(s, &s->cnt[b], N * sizeof(int)))) return rc;
         if ((rc = dalloc(s, &s->key[b], N * sizeof(int)))) return rc;
-        if ((rc = dalloc(s, &s->rank[b], N * sizeof(int)))) return rc;
     }
     if ((rc = dalloc(s, &s->perm, N * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->tmp, N * sizeof(int)))) return rc;
@@ -293,6 +292,8 @@ int alloc_state(tds_sim* s) {
     s->n_tiles = (int)((s->M + tdsk::kScanTile - 1) / tdsk::kScanTile);
     if ((rc = dalloc(s, &s->tile_sum, (size_t)2 * s->n_tiles * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->phi_acc, (size_t)s->R * tdsk::kPhiCopies * 6 * sizeof(unsigned long long)))) return rc;
+    if ((rc = dalloc(s, &s->done, sizeof(unsigned)))) return rc;
+    CK(cudaMemset(s->done, 0, sizeof(unsigned)));
     if ((rc = dalloc(s, &s->status, sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->d_step, sizeof(long long)))) return rc;
     if ((rc = dalloc(s, &s->packed_ids, N * sizeof(int)))) return rc;
@@ -391,7 +392,7 @@ void launch_one_step(tds_sim* s, const real* noise) {
     const int nb = (s->N + 255) / 256;
     {
         KernelTimer kt(s, 1);
-        tdsk::k_scatter<<<nb, 256, 0, st>>>(s->key[o], s->rank[o], s->start, s->tmp, s->N, s->d_step);
+        tdsk::k_scatter<<<nb, 256, 0, st>>>(s->key[o], s->count, s->start, s->tmp, s->N, s->d_step);
     }
     {
         KernelTimer kt(s, 2);
@@ -412,7 +413,6 @@ void launch_one_step(tds_sim* s, const real* noise) {
     a.vel_o = (R2<real>*)s->vel[o];
     a.cnt_o = s->cnt[o];
     a.key_o = s->key[o];
-    a.rank_o = s->rank[o];
     a.key_in = s->key[c];
     a.desc = s->desc;
     a.start = s->start;
@@ -435,12 +435,18 @@ void launch_one_step(tds_sim* s, const real* noise) {
     a.seed = s->seed;
     a.status = s->status;
     a.N = s->N;
+    a.fuse_finalize = s->R <= tdsk::kFuseFinalizeMax;
+    a.R = s->R;
+    a.n_warps = (s->N + 31) / 32;
+    a.done = s->done;
+    a.series = s->series;
+    a.cap_steps = s->series_cap;
     const int ns = (s->N + tdsk::kStepThreads - 1) / tdsk::kStepThreads;
     {
         KernelTimer kt(s, 3);
         tdsk::k_step<real><<<ns, tdsk::kStepThreads, 0, st>>>(a);
     }
-    {
+    if (!a.fuse_finalize) {
         KernelTimer kt(s, 4);
         tdsk::k_finalize<real><<<s->R, 128, 0, st>>>(
             s->phi_acc, (const RepParams<real>*)s->reps, s->R, s->series, 0, s->series_cap, s->d_step);
@@ -526,7 +532,7 @@ int load_state(tds_sim* s, const tds_state_view* in) {
     tdsk::k_prime<real><<<nb, 256, 0, s->stream>>>((const R4<real>*)s->pos[0], s->ids[0],
                                                     (const RepParams<real>*)s->reps, s->local_bits, s->rows,
                                                     s->ivals, s->count, s->tile_sum, s->n_tiles, s->d_step,
-                                                    s->key[0], s->rank[0], s->N, s->status);
+                                                    s->key[0], s->N, s->status);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s->stream));
     return TDS_OK;
@@ -815,7 +821,7 @@ int tds_stream(tds_sim* s, void** stream) {
 
 int tds_kernels_per_step(const tds_sim* s, int* n) {
     if (!s || !n) return TDS_ERR_ARG;
-    *n = 5;
+    *n = s->R <= tdsk::kFuseFinalizeMax ? 4 : 5;
     return TDS_OK;
 }
 

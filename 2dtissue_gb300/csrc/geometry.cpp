@@ -233,7 +233,7 @@ void build_cell_descriptors(const CellLevel& L, std::vector<uint32_t>& desc) {
                     const int dy = e % 3 - 1, dz = e / 3 - 1;
                     if (iy + dy < 0 || iy + dy >= L.gy || iz + dz < 0 || iz + dz >= L.gz) continue;
                     const int rr = (iz + dz) * L.gy + (iy + dy);
-                    int first = -1, fx = 0, len = 0;
+                    int first = -1, fx = 0, lx = 0, len = 0;
                     for (int q = 0; q < L.rows[2 * rr + 1]; ++q) {
                         const int* J = &L.ivals[4 * (L.rows[2 * rr] + q)];
                         const int lo = std::max(J[0], ix - 1), hi = std::min(J[1], ix + 1);
@@ -241,9 +241,13 @@ void build_cell_descriptors(const CellLevel& L, std::vector<uint32_t>& desc) {
                         // ids are consecutive along the row; runs from two intervals are merged
                         if (first < 0) first = J[2] + lo - J[0], fx = lo;
                         len = (J[2] + hi - J[0]) - first + 1;
+                        lx = hi;
                     }
-                    if (first >= 0)
+                    if (first >= 0) {
                         desc[(size_t)id * 12 + e] = ((uint32_t)first << 4) | ((uint32_t)(fx - (ix - 1)) << 2) | (uint32_t)len;
+                        // word 9: bit e set when the run skips a non-surface cell (x -> id is not affine)
+                        if (lx - fx + 1 != len) desc[(size_t)id * 12 + 9] |= 1u << e;
+                    }
                 }
             }
         }

@@ -53,7 +53,8 @@ void build_cell_level(const Mesh& m, double h, const double origin[3], CellLevel
 
 // Per surface cell, the ids of its 27 neighbour cells as 9 x-runs (rows dy, dz in -1..1, in the
 // order r = (dz + 1) * 3 + (dy + 1)); entry = id of the run's first cell << 4 | (x offset of that
-// cell from ix - 1) << 2 | number of cells in the run (0..3). 12 words per cell (3 spare).
+// cell from ix - 1) << 2 | number of cells in the run (0..3); word 9 bit e is set when run e
+// skips a non-surface cell. 12 words per cell (2 spare).
 void build_cell_descriptors(const CellLevel& L, std::vector<uint32_t>& desc);
 
 // Seeded placement: face picked with probability proportional to its 3D area, uniform

@@ -52,6 +52,7 @@ constexpr int kScanItems = 32;
 constexpr int kScanTile = kScanThreads * kScanItems;  // buckets per scan tile
 constexpr int kStepThreads = 256;
 constexpr int kPhiCopies = 32;    // spread the order-parameter atomics over copies
+constexpr int kFuseFinalizeMax = 64;  // replicas finished inside the step kernel
 
 template <typename real>
 struct alignas(4 * sizeof(real)) R4 {
@@ -90,7 +91,6 @@ struct StepArgs {
     R2<real>* vel_o;
     int* cnt_o;
     int* key_o;
-    int* rank_o;
     const int* key_in;  // cell bucket of each particle (sorted order)
     const uint4* desc;  // per-cell neighbour-run descriptors, all levels
     const int* start;
@@ -113,6 +113,11 @@ struct StepArgs {
     unsigned long long seed;
     int* status;
     int N;
+    // order parameter finished by the last warp (replica count <= kFuseFinalizeMax)
+    int fuse_finalize, R, n_warps;
+    unsigned* done;
+    double* series;
+    long long cap_steps;
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -372,10 +377,24 @@ __device__ __forceinline__ int bucket_of(const RepParams<real>& rp, const int2* 
 }
 
 __device__ __forceinline__ void add_tile(int* tile_sum, int key) {
-    // warp-aggregated count of keys per scan tile
+    // warp-aggregated count of keys per scan tile (keys of a warp are nearly always in one tile)
     const int tile = key / kScanTile;
-    const unsigned m = __match_any_sync(__activemask(), tile);
-    if ((threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(&tile_sum[tile], __popc(m));
+    const unsigned act = __activemask();
+    const int leader = __ffs(act) - 1;
+    const int t0 = __shfl_sync(act, tile, leader);
+    if (__all_sync(act, tile == t0)) {
+        if ((int)(threadIdx.x & 31) == leader) atomicAdd(&tile_sum[tile], __popc(act));
+    } else {
+        const unsigned m = __match_any_sync(act, tile);
+        if ((int)(threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(&tile_sum[tile], __popc(m));
+    }
+}
+
+__device__ __forceinline__ unsigned sel9(const unsigned (&e)[9], int i) {
+    unsigned v = e[0];
+#pragma unroll
+    for (int k = 1; k < 9; ++k) v = (i == k) ? e[k] : v;
+    return v;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -384,12 +403,10 @@ __device__ __forceinline__ void add_tile(int* tile_sum, int key) {
 // One neighbour candidate: 3D chord distance test, Szabo force and polarity sums.
 template <typename real>
 __device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<real>& P, const R4<real>& Q,
-                                          const R4<real>* __restrict__ pol, int j, bool self, real (&acc)[6],
-                                          int& cnt) {
+                                          const R4<real>& QL, bool self, real (&acc)[6], int& cnt) {
     const real dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
     const real d2 = dx * dx + dy * dy + dz * dz;
     if (d2 < rp.r_max2 && !self) {
-        const R4<real> QL = pol[j];
         const real rd = d_rsqrt(d2);  // 1/d (d2 > 0 unless two particles coincide)
         const real d = d2 * rd;
         const real fm = d < rp.twoR ? rp.k * (rp.twoR - d) * rp.inv_twoR : -(rp.adh_scale * (d - rp.twoR));
@@ -407,7 +424,7 @@ __device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<re
 }
 
 template <typename real>
-__global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a) {
+__global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs<real> a) {
     typedef R4<real> r4;
     const int q = blockIdx.x * kStepThreads + threadIdx.x;
     const bool active = q < a.N;
@@ -432,10 +449,13 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
         int rs[9], rc[9];
         int total = 0;
         const int id0 = key0 - rp.base;
+        unsigned e[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, gaps = 0x1ffu;
         if (id0 < rp.C) {
             const uint4* dp = a.desc + (size_t)rp.desc_off + (size_t)id0 * 3;
             const uint4 d0 = dp[0], d1 = dp[1], d2 = dp[2];
-            const unsigned e[9] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w, d2.x};
+            e[0] = d0.x, e[1] = d0.y, e[2] = d0.z, e[3] = d0.w, e[4] = d1.x, e[5] = d1.y, e[6] = d1.z, e[7] = d1.w;
+            e[8] = d2.x;
+            gaps = d2.y;
 #pragma unroll
             for (int r = 0; r < 9; ++r) {
                 const int first = (int)(e[r] >> 4), len = (int)(e[r] & 3u);
@@ -450,33 +470,36 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
 #pragma unroll
             for (int r = 0; r < 9; ++r) rs[r] = 0, rc[r] = 0;
         }
-        // pair sums over all candidates (in a fixed order), two per iteration
+        // pair sums over all candidates (in a fixed order), four per iteration; position and
+        // polarity of a candidate are loaded together so that each iteration waits once
         real acc[6] = {0, 0, 0, 0, 0, 0};
         int cnt = 0;
         int r = 0, t = rs[0], left = rc[0];
-        for (int k = 0; k < total; k += 2) {
-            while (left == 0) {
-                ++r;
-                t = rs[r];
-                left = rc[r];
-            }
-            const int ta = t++;
-            --left;
-            int tb = -1;
-            if (k + 1 < total) {
-                while (left == 0) {
-                    ++r;
-                    t = rs[r];
-                    left = rc[r];
+        for (int k = 0; k < total; k += 4) {
+            int tt[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                tt[u] = -1;
+                if (k + u < total) {
+                    while (left == 0) {
+                        ++r;
+                        t = rs[r];
+                        left = rc[r];
+                    }
+                    tt[u] = t++;
+                    --left;
                 }
-                tb = t++;
-                --left;
             }
-            const int tb2 = tb >= 0 ? tb : ta;
-            const r4 Qa = a.pos[ta];
-            const r4 Qb = a.pos[tb2];
-            pair_term(rp, P, Qa, a.pol, ta, ta == q, acc, cnt);
-            if (tb >= 0) pair_term(rp, P, Qb, a.pol, tb, tb == q, acc, cnt);
+            r4 Q[4], QL[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int tu = tt[u] >= 0 ? tt[u] : tt[0];
+                Q[u] = a.pos[tu];
+                QL[u] = a.pol[tu];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (tt[u] >= 0) pair_term(rp, P, Q[u], QL[u], tt[u] == q, acc, cnt);
         }
         const real Fxr = acc[0], Fyr = acc[1], Fzr = acc[2];
         const real mxr = acc[3], myr = acc[4], mzr = acc[5];
@@ -557,11 +580,27 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
         vo.x = vu, vo.y = vv;
         a.vel_o[q] = vo;
         a.cnt_o[q] = cnt;
-        // next step's cell key, rank and scan-tile count (counting sort)
-        bool lost = false;
-        const int key = bucket_of(rp, a.rows, a.ivals, rx, ry, rz, lost);
-        if (lost) st |= ST_CELL;
-        a.rank_o[q] = atomicAdd(&a.count[key], 1);
+        // next step's cell key (from the old cell's descriptor when the new cell is one of its 27
+        // neighbours, else by the row lookup), count and scan-tile count (counting sort)
+        int key = -1;
+        {
+            int jx, jy, jz, ix0, iy0, iz0;
+            cell_coords(rp, rx, ry, rz, jx, jy, jz);
+            cell_coords(rp, P.x, P.y, P.z, ix0, iy0, iz0);
+            const int ddy = jy - iy0, ddz = jz - iz0, xo = jx - ix0 + 1;
+            if (ddy >= -1 && ddy <= 1 && ddz >= -1 && ddz <= 1 && xo >= 0 && xo <= 2) {
+                const int r9 = (ddz + 1) * 3 + (ddy + 1);
+                const unsigned en = sel9(e, r9);
+                const int len = (int)(en & 3u), off = (int)((en >> 2) & 3u), xi = xo - off;
+                if (!((gaps >> r9) & 1u) && xi >= 0 && xi < len) key = rp.base + (int)(en >> 4) + xi;
+            }
+        }
+        if (key < 0) {
+            bool lost = false;
+            key = bucket_of(rp, a.rows, a.ivals, rx, ry, rz, lost);
+            if (lost) st |= ST_CELL;
+        }
+        atomicAdd(&a.count[key], 1);
         a.key_o[q] = key;
         add_tile(a.tile_sum + (size_t)((step + 1) & 1) * a.n_tiles, key);
 
@@ -609,12 +648,43 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
             atomicAdd(&a.phi_acc[((size_t)rep * kPhiCopies + copy) * 6 + k],
                       (unsigned long long)__double2ll_rn((double)ph[k] * ps));
     }
+    if (!a.fuse_finalize) return;
+    // the last warp to finish reduces the copies and writes this step's order parameters
+    unsigned prev = 0;
+    if (lane == 0) {
+        __threadfence();
+        prev = atomicAdd(a.done, 1u);
+    }
+    prev = __shfl_sync(FULL, prev, 0);
+    if (prev != (unsigned)(a.n_warps - 1)) return;
+    __threadfence();
+    for (int r = 0; r < a.R; ++r) {
+        long long v[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            long long x = (long long)atomicExch(&a.phi_acc[((size_t)r * kPhiCopies + lane) * 6 + k], 0ull);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+            v[k] = x;
+        }
+        if (lane == 0) {
+            const RepParams<real>& rr = a.reps[r];
+            const double inv = 1.0 / rr.phiscale;
+            const double L0 = (double)v[0] * inv, L1 = (double)v[1] * inv, L2 = (double)v[2] * inv;
+            const double V0 = (double)v[3] * inv, V1 = (double)v[4] * inv, V2 = (double)v[5] * inv;
+            if (step >= 0 && step < a.cap_steps) {
+                a.series[(size_t)step * 2 * a.R + r] = sqrt(L0 * L0 + L1 * L1 + L2 * L2) * rr.inv_n;
+                a.series[(size_t)step * 2 * a.R + a.R + r] = sqrt(V0 * V0 + V1 * V1 + V2 * V2) * rr.inv_n;
+            }
+        }
+    }
+    if (lane == 0) atomicExch(a.done, 0u);
 }
 
 // ---------------------------------------------------------------------------------------------
 // cell-list kernels
 // ---------------------------------------------------------------------------------------------
-// Exclusive scan of count[0..M) into start[0..M), zeroing count. Each block's base is the sum of
+// Exclusive scan of count[0..M) into start[0..M). Each block's base is the sum of
 // the per-tile counts of the tiles before it (accumulated by the previous step), so no block
 // waits on another. Also zeroes the other parity's tile counts for the step about to run.
 __global__ void __launch_bounds__(kScanThreads) k_scan(int* __restrict__ count, int* __restrict__ start, long long M,
@@ -688,25 +758,25 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(int* __restrict__ count, 
             o.w = run;
             run += v[i + 3];
             *reinterpret_cast<int4*>(start + base + i) = o;
-            *reinterpret_cast<int4*>(count + base + i) = make_int4(0, 0, 0, 0);
         }
     } else {
 #pragma unroll
         for (int i = 0; i < kScanItems; ++i) {
-            if (base + i < M) {
-                start[base + i] = run;
-                count[base + i] = 0;
-            }
+            if (base + i < M) start[base + i] = run;
             run += v[i];
         }
     }
 }
 
-__global__ void k_scatter(const int* __restrict__ key, const int* __restrict__ rank, const int* __restrict__ start,
-                          int* __restrict__ perm, int N, long long* d_step) {
+// Counting-sort scatter; the cell's count is the cursor and ends at zero for the next step.
+__global__ void k_scatter(const int* __restrict__ key, int* __restrict__ count, const int* __restrict__ start,
+                          int* __restrict__ tmp, int N, long long* d_step) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s == 0) *d_step += 1;
-    if (s < N) perm[start[key[s]] + rank[s]] = s;
+    if (s < N) {
+        const int b = key[s];
+        tmp[start[b] + atomicSub(&count[b], 1) - 1] = s;
+    }
 }
 
 // Within each cell, particles in increasing particle-id order: the particle in slot s goes to
@@ -738,7 +808,7 @@ __global__ void k_order(const int* __restrict__ tmp, const int* __restrict__ key
 template <typename real>
 __global__ void k_prime(const R4<real>* pos, const int* ids, const RepParams<real>* reps, int local_bits,
                         const int2* rows, const int4* ivals, int* count, int* tile_sum, int n_tiles,
-                        const long long* d_step, int* key, int* rank, int N, int* status) {
+                        const long long* d_step, int* key, int N, int* status) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= N) return;
     const R4<real> P = pos[s];
@@ -747,7 +817,7 @@ __global__ void k_prime(const R4<real>* pos, const int* ids, const RepParams<rea
     const int k = bucket_of(rp, rows, ivals, P.x, P.y, P.z, lost);
     if (lost) atomicOr(status, ST_CELL);
     key[s] = k;
-    rank[s] = atomicAdd(&count[k], 1);
+    atomicAdd(&count[k], 1);
     add_tile(tile_sum + (size_t)((*d_step + 1) & 1) * n_tiles, k);
 }
 

@@ -5,7 +5,7 @@ Workload (the headline configuration): the (20,10,10) ellipsoid meshed as a leve
 (163,842 vertices, 327,680 faces), 1,048,576 particles at area packing 0.5 (radius from packing,
 r_max = 2.4 R), eta = 0.3, dt = 0.01, FP32 state. Synthetic, seeded placement (no dataset exists).
 
-One bench step = one simulation step of the whole system (5 kernels). L2 is flushed (a 256 MB
+One bench step = one simulation step of the whole system (4 kernels). L2 is flushed (a 256 MB
 write, outside the timed window) before every timed step; each step is timed with CUDA events on
 the handle's stream. value = particle-steps/s over all ranks (max time over ranks).
 e2e = the same metric through the C-ABI with host buffers: set_state (H2D) + tds_step + get_state
@@ -33,7 +33,6 @@ UNIT = "particle-steps/s"
 ALG_BYTES_PARTICLE = 68  # FP32: read uv 8 + theta 4 + face 4 + r3d 12; write those + vel_uv 8 + count 4
 ALG_BYTES_FACE = 60      # 3 UV corners x 8 + 3 3D corners x 12
 ALG_BYTES_REPLICA = 4    # order parameter
-KERNELS_PER_STEP = 5
 
 
 def config2(tg):
@@ -319,7 +318,7 @@ def run_gpu(args):
                 "config": workload_config(mesh, p, n, "flushed (256 MB write) before every timed step"),
                 "roofline": roofline, "step_hbm_frac": step_frac, "kernel_share": shares,
                 "graph_loop": {"value": loop_rate, "unit": UNIT, "note": "128 graph-captured steps, no flush"},
-                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": KERNELS_PER_STEP * args.steps, "clocks": clocks,
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": sim.kernels_per_step() * args.steps, "clocks": clocks,
                 "parallelism": "replicas only (one independent 1M-particle system per GPU)"}
         print(json.dumps(line), flush=True)
     sim.close()
