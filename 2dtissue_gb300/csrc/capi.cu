@@ -88,7 +88,6 @@ struct tds_sim {
     int* start = nullptr;
     int* count = nullptr;
     unsigned long long* phi_acc = nullptr;
-    unsigned* done = nullptr;  // warps finished in the current step kernel (fused order parameter)
     double* series = nullptr;
     long long series_cap = 0;  // steps
     int* status = nullptr;
@@ -292,8 +291,6 @@ int alloc_state(tds_sim* s) {
     s->n_tiles = (int)((s->M + tdsk::kScanTile - 1) / tdsk::kScanTile);
     if ((rc = dalloc(s, &s->tile_sum, (size_t)2 * s->n_tiles * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->phi_acc, (size_t)s->R * tdsk::kPhiCopies * 6 * sizeof(unsigned long long)))) return rc;
-    if ((rc = dalloc(s, &s->done, sizeof(unsigned)))) return rc;
-    CK(cudaMemset(s->done, 0, sizeof(unsigned)));
     if ((rc = dalloc(s, &s->status, sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->d_step, sizeof(long long)))) return rc;
     if ((rc = dalloc(s, &s->packed_ids, N * sizeof(int)))) return rc;
@@ -435,18 +432,12 @@ void launch_one_step(tds_sim* s, const real* noise) {
     a.seed = s->seed;
     a.status = s->status;
     a.N = s->N;
-    a.fuse_finalize = s->R <= tdsk::kFuseFinalizeMax;
-    a.R = s->R;
-    a.n_warps = (s->N + 31) / 32;
-    a.done = s->done;
-    a.series = s->series;
-    a.cap_steps = s->series_cap;
     const int ns = (s->N + tdsk::kStepThreads - 1) / tdsk::kStepThreads;
     {
         KernelTimer kt(s, 3);
         tdsk::k_step<real><<<ns, tdsk::kStepThreads, 0, st>>>(a);
     }
-    if (!a.fuse_finalize) {
+    {
         KernelTimer kt(s, 4);
         tdsk::k_finalize<real><<<s->R, 128, 0, st>>>(
             s->phi_acc, (const RepParams<real>*)s->reps, s->R, s->series, 0, s->series_cap, s->d_step);
@@ -821,7 +812,7 @@ int tds_stream(tds_sim* s, void** stream) {
 
 int tds_kernels_per_step(const tds_sim* s, int* n) {
     if (!s || !n) return TDS_ERR_ARG;
-    *n = s->R <= tdsk::kFuseFinalizeMax ? 4 : 5;
+    *n = 5;
     return TDS_OK;
 }
 

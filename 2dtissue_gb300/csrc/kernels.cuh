@@ -52,7 +52,6 @@ constexpr int kScanItems = 32;
 constexpr int kScanTile = kScanThreads * kScanItems;  // buckets per scan tile
 constexpr int kStepThreads = 256;
 constexpr int kPhiCopies = 32;    // spread the order-parameter atomics over copies
-constexpr int kFuseFinalizeMax = 64;  // replicas finished inside the step kernel
 
 template <typename real>
 struct alignas(4 * sizeof(real)) R4 {
@@ -113,11 +112,6 @@ struct StepArgs {
     unsigned long long seed;
     int* status;
     int N;
-    // order parameter finished by the last warp (replica count <= kFuseFinalizeMax)
-    int fuse_finalize, R, n_warps;
-    unsigned* done;
-    double* series;
-    long long cap_steps;
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -403,10 +397,12 @@ __device__ __forceinline__ unsigned sel9(const unsigned (&e)[9], int i) {
 // One neighbour candidate: 3D chord distance test, Szabo force and polarity sums.
 template <typename real>
 __device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<real>& P, const R4<real>& Q,
-                                          const R4<real>& QL, bool self, real (&acc)[6], int& cnt) {
+                                          const R4<real>* __restrict__ pol, int j, bool self, real (&acc)[6],
+                                          int& cnt) {
     const real dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
     const real d2 = dx * dx + dy * dy + dz * dz;
     if (d2 < rp.r_max2 && !self) {
+        const R4<real> QL = pol[j];  // polarity only for neighbours (about a third of candidates)
         const real rd = d_rsqrt(d2);  // 1/d (d2 > 0 unless two particles coincide)
         const real d = d2 * rd;
         const real fm = d < rp.twoR ? rp.k * (rp.twoR - d) * rp.inv_twoR : -(rp.adh_scale * (d - rp.twoR));
@@ -424,7 +420,7 @@ __device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<re
 }
 
 template <typename real>
-__global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs<real> a) {
+__global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a) {
     typedef R4<real> r4;
     const int q = blockIdx.x * kStepThreads + threadIdx.x;
     const bool active = q < a.N;
@@ -470,36 +466,32 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs<real> a
 #pragma unroll
             for (int r = 0; r < 9; ++r) rs[r] = 0, rc[r] = 0;
         }
-        // pair sums over all candidates (in a fixed order), four per iteration; position and
-        // polarity of a candidate are loaded together so that each iteration waits once
+        // pair sums over all candidates (in a fixed order), two per iteration
         real acc[6] = {0, 0, 0, 0, 0, 0};
         int cnt = 0;
         int r = 0, t = rs[0], left = rc[0];
-        for (int k = 0; k < total; k += 4) {
-            int tt[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                tt[u] = -1;
-                if (k + u < total) {
-                    while (left == 0) {
-                        ++r;
-                        t = rs[r];
-                        left = rc[r];
-                    }
-                    tt[u] = t++;
-                    --left;
+        for (int k = 0; k < total; k += 2) {
+            while (left == 0) {
+                ++r;
+                t = rs[r];
+                left = rc[r];
+            }
+            const int ta = t++;
+            --left;
+            int tb = -1;
+            if (k + 1 < total) {
+                while (left == 0) {
+                    ++r;
+                    t = rs[r];
+                    left = rc[r];
                 }
+                tb = t++;
+                --left;
             }
-            r4 Q[4], QL[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int tu = tt[u] >= 0 ? tt[u] : tt[0];
-                Q[u] = a.pos[tu];
-                QL[u] = a.pol[tu];
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (tt[u] >= 0) pair_term(rp, P, Q[u], QL[u], tt[u] == q, acc, cnt);
+            const r4 Qa = a.pos[ta];
+            const r4 Qb = a.pos[tb >= 0 ? tb : ta];
+            pair_term(rp, P, Qa, a.pol, ta, ta == q, acc, cnt);
+            if (tb >= 0) pair_term(rp, P, Qb, a.pol, tb, tb == q, acc, cnt);
         }
         const real Fxr = acc[0], Fyr = acc[1], Fzr = acc[2];
         const real mxr = acc[3], myr = acc[4], mzr = acc[5];
@@ -648,37 +640,6 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs<real> a
             atomicAdd(&a.phi_acc[((size_t)rep * kPhiCopies + copy) * 6 + k],
                       (unsigned long long)__double2ll_rn((double)ph[k] * ps));
     }
-    if (!a.fuse_finalize) return;
-    // the last warp to finish reduces the copies and writes this step's order parameters
-    unsigned prev = 0;
-    if (lane == 0) {
-        __threadfence();
-        prev = atomicAdd(a.done, 1u);
-    }
-    prev = __shfl_sync(FULL, prev, 0);
-    if (prev != (unsigned)(a.n_warps - 1)) return;
-    __threadfence();
-    for (int r = 0; r < a.R; ++r) {
-        long long v[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            long long x = (long long)atomicExch(&a.phi_acc[((size_t)r * kPhiCopies + lane) * 6 + k], 0ull);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
-            v[k] = x;
-        }
-        if (lane == 0) {
-            const RepParams<real>& rr = a.reps[r];
-            const double inv = 1.0 / rr.phiscale;
-            const double L0 = (double)v[0] * inv, L1 = (double)v[1] * inv, L2 = (double)v[2] * inv;
-            const double V0 = (double)v[3] * inv, V1 = (double)v[4] * inv, V2 = (double)v[5] * inv;
-            if (step >= 0 && step < a.cap_steps) {
-                a.series[(size_t)step * 2 * a.R + r] = sqrt(L0 * L0 + L1 * L1 + L2 * L2) * rr.inv_n;
-                a.series[(size_t)step * 2 * a.R + a.R + r] = sqrt(V0 * V0 + V1 * V1 + V2 * V2) * rr.inv_n;
-            }
-        }
-    }
-    if (lane == 0) atomicExch(a.done, 0u);
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -5,7 +5,7 @@ Workload (the headline configuration): the (20,10,10) ellipsoid meshed as a leve
 (163,842 vertices, 327,680 faces), 1,048,576 particles at area packing 0.5 (radius from packing,
 r_max = 2.4 R), eta = 0.3, dt = 0.01, FP32 state. Synthetic, seeded placement (no dataset exists).
 
-One bench step = one simulation step of the whole system (4 kernels). L2 is flushed (a 256 MB
+One bench step = one simulation step of the whole system (5 kernels). L2 is flushed (a 256 MB
 write, outside the timed window) before every timed step; each step is timed with CUDA events on
 the handle's stream. value = particle-steps/s over all ranks (max time over ranks).
 e2e = the same metric through the C-ABI with host buffers: set_state (H2D) + tds_step + get_state
