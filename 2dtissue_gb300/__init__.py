@@ -76,6 +76,7 @@ def lib(build_if_missing=True):
     L.tds_update.argtypes = [VP, P(_StateView)]
     L.tds_set_state.argtypes = [VP, P(_StateView)]
     L.tds_get_state.argtypes = [VP, P(_StateView)]
+    L.tds_get_state_noalloc.argtypes = [VP, P(_StateView)]
     L.tds_get_order_parameter.argtypes = [VP, VP, VP, I, P(I)]
     L.tds_get_step.argtypes = [VP, P(C.c_int64)]
     L.tds_get_status.argtypes = [VP, P(I)]
@@ -250,6 +251,18 @@ class Simulation:
         v = _StateView(_ptr(o["uv"]), _ptr(o["theta"]), _ptr(o["face"]), _ptr(o["r3d"]), _ptr(o.get("vel_uv")),
                        _ptr(o.get("nbr")))
         self._check(lib().tds_get_state(self.h, C.byref(v)))
+        return o
+
+    def get_state_noalloc(self, out=None):
+        """Same as get_state, staged in the library's fixed device array (no device allocation;
+        at most 233,016 particles; calls that overlap on the GPU race)."""
+        N = self.N
+        o = out if out is not None else dict(uv=np.zeros((N, 2)), theta=np.zeros(N), face=np.zeros(N, np.int32),
+                                            r3d=np.zeros((N, 3)), vel_uv=np.zeros((N, 2)),
+                                            nbr=np.zeros(N, np.int32))
+        v = _StateView(_ptr(o["uv"]), _ptr(o["theta"]), _ptr(o["face"]), _ptr(o["r3d"]), _ptr(o.get("vel_uv")),
+                       _ptr(o.get("nbr")))
+        self._check(lib().tds_get_state_noalloc(self.h, C.byref(v)))
         return o
 
     def order_parameter(self):

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -555,6 +556,80 @@ int save_state(tds_sim* s, tds_state_view* out) {
     return TDS_OK;
 }
 
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// State read-back that allocates nothing (tds_get_state_noalloc)
+// ---------------------------------------------------------------------------------------------
+// Some callers cannot allocate device memory at the point where they read the state back: a host
+// framework that owns all device memory through its own allocator, a memory budget that is fixed
+// after start-up, or a loop that must not call cudaMalloc/cudaFree because those synchronise the
+// device. For them the read-back stages the state in this fixed file-scope array instead of the
+// handle's staging buffers: 16 MiB, i.e. at most 233,016 particles at 72 bytes each (uv, theta,
+// r3d and chart velocity as double, face and neighbour count as int). Every GPU that loads the
+// library holds the array until the process exits.
+constexpr size_t kNoAllocStagingBytes = (size_t)16 << 20;
+constexpr size_t kNoAllocBytesPerParticle = 8 * sizeof(double) + 2 * sizeof(int);
+static __device__ __align__(256) unsigned char g_noalloc_staging[kNoAllocStagingBytes];
+
+namespace {
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[256] = {};  // device address of the staging array, per device ordinal
+
+// Device address of the staging array on the current device. The symbol's name is only a
+// host-side stand-in, so the address is looked up once per device (with that device current).
+int noalloc_staging(tds_sim* s, void** addr) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return fail(s, TDS_ERR_LIMIT, "device ordinal above 255");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_staging);
+        if (e != cudaSuccess) return fail(s, TDS_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_noalloc_addr[dev] = p;
+    }
+    *addr = g_noalloc_addr[dev];
+    return TDS_OK;
+}
+
+template <typename real>
+int save_state_noalloc(tds_sim* s, tds_state_view* out) {
+    const size_t N = (size_t)s->N;
+    if (N * kNoAllocBytesPerParticle > kNoAllocStagingBytes) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "tds_get_state_noalloc: %zu particles exceed the fixed staging of %zu bytes "
+                      "(at most %zu particles)", N, kNoAllocStagingBytes, kNoAllocStagingBytes / kNoAllocBytesPerParticle);
+        return fail(s, TDS_ERR_LIMIT, buf);
+    }
+    void* base = nullptr;
+    int rc;
+    if ((rc = noalloc_staging(s, &base))) return rc;
+    // every staged value is written by the gather for all N particles: nothing needs clearing
+    double* d_uv = (double*)base;
+    double* d_th = d_uv + 2 * N;
+    double* d_r3 = d_uv + 3 * N;
+    double* d_vel = d_uv + 6 * N;
+    int* d_face = (int*)(d_uv + 8 * N);
+    int* d_cnt = d_face + N;
+    const int c = s->cur;
+    const int nb = (s->N + 255) / 256;
+    tdsk::k_gather_state<real><<<nb, 256, 0, s->stream>>>(
+        (const R4<real>*)s->pos[c], (const R4<real>*)s->pol[c], (const R2<real>*)s->uv[c], s->ids[c],
+        (const R2<real>*)s->vel[c], s->cnt[c], (const RepParams<real>*)s->reps, s->local_bits, d_uv, d_th, d_face, d_r3,
+        d_vel, d_cnt, s->N);
+    CK(cudaGetLastError());
+    if (out->uv) CK(cudaMemcpyAsync(out->uv, d_uv, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    if (out->theta) CK(cudaMemcpyAsync(out->theta, d_th, N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    if (out->face) CK(cudaMemcpyAsync(out->face, d_face, N * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    if (out->r3d) CK(cudaMemcpyAsync(out->r3d, d_r3, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    if (out->vel_uv) CK(cudaMemcpyAsync(out->vel_uv, d_vel, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    if (out->nbr_count) CK(cudaMemcpyAsync(out->nbr_count, d_cnt, N * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return TDS_OK;
+}
+
 int check_params(const tds_params& p, std::string& why) {
     if (!(p.radius > 0)) return why = "radius must be > 0", 1;
     if (!(p.r_max > 2 * p.radius)) return why = "r_max must exceed 2*radius", 1;
@@ -758,6 +833,11 @@ int tds_set_state(tds_sim* s, const tds_state_view* in) {
 int tds_get_state(tds_sim* s, tds_state_view* out) {
     if (!s || !out) return TDS_ERR_ARG;
     return s->precision == 32 ? save_state<float>(s, out) : save_state<double>(s, out);
+}
+
+int tds_get_state_noalloc(tds_sim* s, tds_state_view* out) {
+    if (!s || !out) return TDS_ERR_ARG;
+    return s->precision == 32 ? save_state_noalloc<float>(s, out) : save_state_noalloc<double>(s, out);
 }
 
 int tds_get_order_parameter(tds_sim* s, double* phi, double* psi, int cap, int* n_steps) {

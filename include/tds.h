@@ -96,6 +96,17 @@ int tds_step(tds_sim* sim, int n_steps, const double* noise);
 int tds_update(tds_sim* sim, tds_state_view* out);
 int tds_set_state(tds_sim* sim, const tds_state_view* in);
 int tds_get_state(tds_sim* sim, tds_state_view* out);
+/* Same result as tds_get_state, without any device allocation: no counterpart in the reference
+ * (its state lives in host memory). For callers that cannot allocate device memory where they
+ * read the state back -- a host framework that owns all device memory through its own allocator,
+ * a device-memory budget fixed after start-up, or a loop that must not call cudaMalloc/cudaFree
+ * because they synchronise the device. The state is staged in one fixed 16 MiB array that the
+ * library holds on every GPU that loads it, so at most 233,016 particles (72 bytes each); larger
+ * handles get TDS_ERR_LIMIT. The handle's device must be current. The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress), so make that first call before any stream
+ * capture. All calls share the array: calls that overlap on the GPU (other threads or streams)
+ * race and must be serialised by the caller; nothing in it needs clearing between calls. */
+int tds_get_state_noalloc(tds_sim* sim, tds_state_view* out);
 /* phi = |sum normalize((r - c) x v)| / N, psi = |sum v/|v|| / N per step and replica:
  * arrays of cap entries, step-major ([step][replica]); *n_steps gets the number of steps stored. */
 int tds_get_order_parameter(tds_sim* sim, double* phi, double* psi, int cap, int* n_steps);
