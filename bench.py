@@ -324,6 +324,61 @@ def run_gpu(args):
     sim.close()
 
 
+def run_ensemble(args):
+    """Batched ragged ensemble (4096 replicas on the (4,2,2) ellipsoid, level-4 icosphere,
+    particle counts log-uniform in [64, 8192], eta in [0, 2 pi], v0 in [0.5, 1.5], dt = 0.02) in one
+    handle, against the same replicas launched one by one with plain handles (a seeded sample of
+    replicas, per-replica launches interleaved step by step). Working set > L2: no flush needed."""
+    import torch
+    tg = importlib.import_module("2dtissue_gb300")
+    ens = importlib.import_module("2dtissue_gb300.ensemble")
+    mesh = tg.Mesh.ellipsoid(4, (4.0, 2.0, 2.0))
+    n, eta, v0 = ens.config3_replicas(seed=0, n_replicas=args.replicas)
+    ps = [tg.Params(radius=0.05, r_max=0.12, v0=float(v), eta=float(e), dt=0.02) for e, v in zip(eta, v0)]
+    sim = tg.Simulation(mesh, ps, [int(x) for x in n], seed=0, precision=32)
+    sim.start()
+    stream = torch.cuda.ExternalStream(sim.stream())
+    sim.step(max(args.warmup, 3))
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    sim.step_async(args.steps)
+    b.record(stream)
+    torch.cuda.synchronize()
+    assert sim.status() == 0
+    batched = int(n.sum()) * args.steps / (a.elapsed_time(b) * 1e-3)
+    phi, psi = sim.order_parameter()
+    sim.close()
+    # one by one: a seeded sample of replicas, each its own plain handle
+    sample = np.sort(np.random.default_rng(1).choice(len(n), min(args.sample, len(n)), replace=False))
+    sims = [tg.Simulation(mesh, ps[i], int(n[i]), seed=int(i), precision=32) for i in sample]
+    for s_ in sims:
+        s_.start()
+        s_.step(3)
+    torch.cuda.synchronize()
+    steps1 = max(3, args.steps // 10)
+    t0 = time.perf_counter()
+    for _ in range(steps1):
+        for s_ in sims:
+            s_.step_async(1)
+    torch.cuda.synchronize()
+    one_by_one = int(n[sample].sum()) * steps1 / (time.perf_counter() - t0)
+    for s_ in sims:
+        assert s_.status() == 0
+        s_.close()
+    line = {"metric": "particle-steps/s (ragged ensemble, %d replicas)" % len(n), "value": batched, "unit": UNIT,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic (seeded)", "config": {"workload": "ensemble, (4,2,2) ellipsoid L4, N log-uniform "
+                                                  "[64,8192], eta U[0,2pi], v0 U[0.5,1.5]",
+                                                  "replicas": len(n), "particles": int(n.sum()),
+                                                  "l2": "inputs larger than L2 (no flush)"},
+            "one_by_one": {"value": one_by_one, "replicas_sampled": len(sample), "steps": steps1},
+            "batched_over_one_by_one": batched / one_by_one,
+            "order_parameter_series": {"steps": int(phi.shape[0]), "replicas": int(phi.shape[1]),
+                                       "mean_phi_last": float(phi[-1].mean())}}
+    print(json.dumps(line), flush=True)
+
+
 def run_profile(args):
     """Minimal driver for ncu: the config-2 system, `warmup` steps, then `steps` steps; no timing."""
     import torch
@@ -346,9 +401,14 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", action="store_true", help="only run warmup + steps (for ncu)")
+    ap.add_argument("--workload", default="plain", choices=["plain", "ensemble"])
+    ap.add_argument("--replicas", type=int, default=4096, help="ensemble workload: replicas")
+    ap.add_argument("--sample", type=int, default=256, help="ensemble workload: replicas run one by one")
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)
+    if args.workload == "ensemble" and args.impl != "reference":
+        return run_ensemble(args)
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":
