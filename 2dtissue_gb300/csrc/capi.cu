@@ -502,9 +502,11 @@ template <typename real>
 int load_state(tds_sim* s, const tds_state_view* in) {
     const size_t N = (size_t)s->N;
     if (!in || !in->uv || !in->theta) return fail(s, TDS_ERR_ARG, "set_state needs uv and theta");
-    if (in->face)
-        for (size_t i = 0; i < N; ++i)
-            if (in->face[i] >= s->mesh->t.F) return fail(s, TDS_ERR_ARG, "set_state: face index out of range");
+    if (in->face) {
+        int fmax = -1;  // branch-free maximum: the compiler vectorises it
+        for (size_t i = 0; i < N; ++i) fmax = std::max(fmax, in->face[i]);
+        if (fmax >= s->mesh->t.F) return fail(s, TDS_ERR_ARG, "set_state: face index out of range");
+    }
     double* d_uv = s->st_d;
     double* d_th = s->st_d + 2 * N;
     double* d_r3 = s->st_d + 3 * N;
@@ -515,16 +517,15 @@ int load_state(tds_sim* s, const tds_state_view* in) {
     if (in->r3d) CK(cudaMemcpyAsync(d_r3, in->r3d, 3 * N * sizeof(double), cudaMemcpyHostToDevice, s->stream));
     s->cur = 0;
     const int nb = (s->N + 255) / 256;
-    tdsk::k_load_state<real><<<nb, 256, 0, s->stream>>>(
-        d_uv, d_th, d_face, d_r3, in->face != nullptr, in->r3d != nullptr, (const real*)s->rec, s->adj, s->G,
-        s->bin_start, s->bin_faces, s->packed_ids, (R4<real>*)s->pos[0], (R4<real>*)s->pol[0], (R2<real>*)s->uv[0],
-        s->ids[0], (R2<real>*)s->vel[0], s->cnt[0], s->N, s->status);
     CK(cudaMemsetAsync(s->count, 0, (size_t)s->M * sizeof(int), s->stream));
     CK(cudaMemsetAsync(s->tile_sum, 0, (size_t)2 * s->n_tiles * sizeof(int), s->stream));
-    tdsk::k_prime<real><<<nb, 256, 0, s->stream>>>((const R4<real>*)s->pos[0], s->ids[0],
-                                                    (const RepParams<real>*)s->reps, s->local_bits, s->rows,
-                                                    s->ivals, s->count, s->tile_sum, s->n_tiles, s->d_step,
-                                                    s->key[0], s->N, s->status);
+    tdsk::k_load_state<real><<<nb, 256, 0, s->stream>>>(
+        d_uv, d_th, d_face, d_r3, in->face != nullptr, in->r3d != nullptr, (const real*)s->rec, s->adj, s->G,
+        s->bin_start, s->bin_faces, s->packed_ids, (const RepParams<real>*)s->reps, s->local_bits, s->rows, s->ivals,
+        (R4<real>*)s->pos[0], (R4<real>*)s->pol[0], (R2<real>*)s->uv[0], s->ids[0], (R2<real>*)s->vel[0], s->cnt[0],
+        s->key[0], s->count, s->N, s->status);
+    tdsk::k_tile_sums<<<s->n_tiles, tdsk::kScanThreads, 0, s->stream>>>(s->count, s->M, s->tile_sum, s->n_tiles,
+                                                                         s->d_step);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s->stream));
     return TDS_OK;

@@ -384,13 +384,6 @@ __device__ __forceinline__ void add_tile(int* tile_sum, int key) {
     }
 }
 
-__device__ __forceinline__ unsigned sel9(const unsigned (&e)[9], int i) {
-    unsigned v = e[0];
-#pragma unroll
-    for (int k = 1; k < 9; ++k) v = (i == k) ? e[k] : v;
-    return v;
-}
-
 // ---------------------------------------------------------------------------------------------
 // k_step
 // ---------------------------------------------------------------------------------------------
@@ -420,7 +413,7 @@ __device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<re
 }
 
 template <typename real>
-__global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a) {
+__global__ void __launch_bounds__(kStepThreads, sizeof(real) == 4 ? 5 : 3) k_step(const StepArgs<real> a) {
     typedef R4<real> r4;
     const int q = blockIdx.x * kStepThreads + threadIdx.x;
     const bool active = q < a.N;
@@ -445,13 +438,10 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
         int rs[9], rc[9];
         int total = 0;
         const int id0 = key0 - rp.base;
-        unsigned e[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, gaps = 0x1ffu;
         if (id0 < rp.C) {
             const uint4* dp = a.desc + (size_t)rp.desc_off + (size_t)id0 * 3;
             const uint4 d0 = dp[0], d1 = dp[1], d2 = dp[2];
-            e[0] = d0.x, e[1] = d0.y, e[2] = d0.z, e[3] = d0.w, e[4] = d1.x, e[5] = d1.y, e[6] = d1.z, e[7] = d1.w;
-            e[8] = d2.x;
-            gaps = d2.y;
+            const unsigned e[9] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w, d2.x};
 #pragma unroll
             for (int r = 0; r < 9; ++r) {
                 const int first = (int)(e[r] >> 4), len = (int)(e[r] & 3u);
@@ -582,9 +572,14 @@ __global__ void __launch_bounds__(kStepThreads, 4) k_step(const StepArgs<real> a
             const int ddy = jy - iy0, ddz = jz - iz0, xo = jx - ix0 + 1;
             if (ddy >= -1 && ddy <= 1 && ddz >= -1 && ddz <= 1 && xo >= 0 && xo <= 2) {
                 const int r9 = (ddz + 1) * 3 + (ddy + 1);
-                const unsigned en = sel9(e, r9);
-                const int len = (int)(en & 3u), off = (int)((en >> 2) & 3u), xi = xo - off;
-                if (!((gaps >> r9) & 1u) && xi >= 0 && xi < len) key = rp.base + (int)(en >> 4) + xi;
+                if (id0 < rp.C) {
+                    // the one descriptor word needed, re-read (L1) rather than kept live in
+                    // registers across the pair loop
+                    const unsigned* dw = reinterpret_cast<const unsigned*>(a.desc + (size_t)rp.desc_off + (size_t)id0 * 3);
+                    const unsigned en = dw[r9], gp = dw[9];
+                    const int len = (int)(en & 3u), off = (int)((en >> 2) & 3u), xi = xo - off;
+                    if (!((gp >> r9) & 1u) && xi >= 0 && xi < len) key = rp.base + (int)(en >> 4) + xi;
+                }
             }
         }
         if (key < 0) {
@@ -764,22 +759,32 @@ __global__ void k_order(const int* __restrict__ tmp, const int* __restrict__ key
     skey[d] = b;
 }
 
-// Cell keys, ranks and tile counts of the current state (after start / set_state); counts and
-// tile counts must be zero.
-template <typename real>
-__global__ void k_prime(const R4<real>* pos, const int* ids, const RepParams<real>* reps, int local_bits,
-                        const int2* rows, const int4* ivals, int* count, int* tile_sum, int n_tiles,
-                        const long long* d_step, int* key, int N, int* status) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= N) return;
-    const R4<real> P = pos[s];
-    const RepParams<real>& rp = reps[(unsigned)ids[s] >> local_bits];
-    bool lost = false;
-    const int k = bucket_of(rp, rows, ivals, P.x, P.y, P.z, lost);
-    if (lost) atomicOr(status, ST_CELL);
-    key[s] = k;
-    atomicAdd(&count[k], 1);
-    add_tile(tile_sum + (size_t)((*d_step + 1) & 1) * n_tiles, k);
+// Per-tile sums of the cell counts (one block per scan tile), written into the tile counts of the
+// parity the next k_scan reads. Used after a state load, where the counts come from k_load_state.
+__global__ void __launch_bounds__(kScanThreads) k_tile_sums(const int* __restrict__ count, long long M,
+                                                            int* __restrict__ tile_sum, int n_tiles,
+                                                            const long long* d_step) {
+    __shared__ int s_warp[kScanThreads / 32];
+    const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
+    int sum = 0;
+    if (base + kScanItems <= M) {
+#pragma unroll
+        for (int i = 0; i < kScanItems; i += 4) {
+            const int4 x = *reinterpret_cast<const int4*>(count + base + i);
+            sum += x.x + x.y + x.z + x.w;
+        }
+    } else {
+        for (int i = 0; i < kScanItems; ++i) sum += base + i < M ? count[base + i] : 0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int b = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) b += s_warp[w];
+        tile_sum[(size_t)((*d_step + 1) & 1) * n_tiles + blockIdx.x] = b;
+    }
 }
 
 // Order parameter of the step just taken, per replica (one block per replica); zeroes the
@@ -834,12 +839,14 @@ __global__ void k_gather_state(const R4<real>* pos, const R4<real>* pol, const R
 }
 
 // Loads a state given in id order (double) into slots = global index; locates faces that are
-// < 0, maps r3d when it is not given, derives the 3D polarity.
+// < 0, maps r3d when it is not given, derives the 3D polarity, and counts the particle into its
+// cell bucket for the next step's counting sort (counts must be zero on entry).
 template <typename real>
 __global__ void k_load_state(const double* i_uv, const double* i_th, const int* i_face, const double* i_r3d,
                              int has_face, int has_r3d, const real* rec, const int4* adj, int G, const int* bs,
-                             const int* bf, const int* packed_ids, R4<real>* pos, R4<real>* pol, R2<real>* uv,
-                             int* ids, R2<real>* vel, int* cnt, int N, int* status) {
+                             const int* bf, const int* packed_ids, const RepParams<real>* reps, int local_bits,
+                             const int2* rows, const int4* ivals, R4<real>* pos, R4<real>* pol, R2<real>* uv,
+                             int* ids, R2<real>* vel, int* cnt, int* key, int* count, int N, int* status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const real u = (real)i_uv[2 * i], v = (real)i_uv[2 * i + 1];
@@ -865,11 +872,17 @@ __global__ void k_load_state(const double* i_uv, const double* i_th, const int* 
     R2<real> U;
     U.x = u, U.y = v;
     uv[i] = U;
-    ids[i] = packed_ids[i];
+    const int id = packed_ids[i];
+    ids[i] = id;
     R2<real> Z;
     Z.x = 0, Z.y = 0;
     vel[i] = Z;
     cnt[i] = 0;
+    bool lost = false;
+    const int k = bucket_of(reps[(unsigned)id >> local_bits], rows, ivals, P.x, P.y, P.z, lost);
+    if (lost) atomicOr(status, ST_CELL);
+    key[i] = k;
+    atomicAdd(&count[k], 1);
 }
 
 template <typename real>

@@ -183,7 +183,7 @@ def test_ensemble_parity(tg, orc, mesh_l4, cfg1):
 
 
 def test_deterministic_replay(tg, mesh_l4):
-    """Order-independent (fixed-point) pair sums: two runs are bitwise identical."""
+    """Particles of a cell in id order and a fixed candidate order: two runs are bitwise identical."""
     outs = []
     for _ in range(2):
         sim = tg.Simulation(mesh_l4, tg.Params(), 3000, seed=9, precision=32)
