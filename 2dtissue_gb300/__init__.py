@@ -77,6 +77,9 @@ def lib(build_if_missing=True):
     L.tds_set_state.argtypes = [VP, P(_StateView)]
     L.tds_get_state.argtypes = [VP, P(_StateView)]
     L.tds_get_state_noalloc.argtypes = [VP, P(_StateView)]
+    L.tds_set_state_async.argtypes = [VP, P(_StateView)]
+    L.tds_get_state_async.argtypes = [VP, P(_StateView)]
+    L.tds_sync.argtypes = [VP]
     L.tds_get_order_parameter.argtypes = [VP, VP, VP, I, P(I)]
     L.tds_get_step.argtypes = [VP, P(C.c_int64)]
     L.tds_get_status.argtypes = [VP, P(I)]
@@ -186,6 +189,7 @@ class Simulation:
 
     def __init__(self, mesh, params, n_particles, seed=0, precision=32):
         self.mesh = mesh
+        self._pending = []  # host arrays of enqueued transfers, held until sync()
         L = lib()
         h = C.c_void_p()
         if np.ndim(n_particles) == 0:
@@ -252,6 +256,38 @@ class Simulation:
                        _ptr(o.get("nbr")))
         self._check(lib().tds_get_state(self.h, C.byref(v)))
         return o
+
+    def set_state_async(self, uv, theta, face=None, r3d=None):
+        """Enqueues set_state (upload stream + load on the compute stream) and returns; the
+        arrays are held until sync()."""
+        uv = np.ascontiguousarray(uv, np.float64)
+        th = np.ascontiguousarray(theta, np.float64)
+        fc = None if face is None else np.ascontiguousarray(face, np.int32)
+        r3 = None if r3d is None else np.ascontiguousarray(r3d, np.float64)
+        self._pending.append((uv, th, fc, r3))
+        v = _StateView(_ptr(uv), _ptr(th), _ptr(fc), _ptr(r3), None, None)
+        self._check(lib().tds_set_state_async(self.h, C.byref(v)))
+
+    def get_state_async(self, out):
+        """Enqueues get_state into the preallocated arrays of `out` (gather on the compute
+        stream, download stream for the copies); they are valid after sync()."""
+        for k, dt, per in (("uv", np.float64, 2), ("theta", np.float64, 1), ("face", np.int32, 1),
+                           ("r3d", np.float64, 3), ("vel_uv", np.float64, 2), ("nbr", np.int32, 1)):
+            a = out.get(k)
+            if a is not None and not (a.flags.c_contiguous and a.dtype == dt and a.size == per * self.N):
+                raise ValueError("get_state_async: out[%r] must be a C-contiguous %s array of %d values"
+                                 % (k, np.dtype(dt).name, per * self.N))
+        self._pending.append(out)
+        v = _StateView(_ptr(out.get("uv")), _ptr(out.get("theta")), _ptr(out.get("face")), _ptr(out.get("r3d")),
+                       _ptr(out.get("vel_uv")), _ptr(out.get("nbr")))
+        self._check(lib().tds_get_state_async(self.h, C.byref(v)))
+
+    def sync(self):
+        """Waits for everything enqueued on this handle; raises on a non-zero device status."""
+        try:
+            self._check(lib().tds_sync(self.h))
+        finally:
+            self._pending = []
 
     def get_state_noalloc(self, out=None):
         """Same as get_state, staged in the library's fixed device array (no device allocation;

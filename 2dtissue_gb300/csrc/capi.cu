@@ -96,8 +96,14 @@ struct tds_sim {
     int* packed_ids = nullptr;
     void* noise = nullptr;
     size_t noise_cap = 0;
-    double* st_d = nullptr;  // staging (double) 8N
-    int* st_i = nullptr;     // staging (int) 2N
+    double* st_d = nullptr;  // output staging (double) 8N
+    int* st_i = nullptr;     // output staging (int) 2N
+    double* in_d = nullptr;  // input staging (double) 6N
+    int* in_i = nullptr;     // input staging (int) N
+    // state transfers: uploads and downloads on their own streams, so that the two directions of
+    // the host link run at the same time; events order them against the compute stream
+    cudaStream_t up = nullptr, down = nullptr;
+    cudaEvent_t ev_in_ready = nullptr, ev_in_free = nullptr, ev_out_ready = nullptr, ev_out_free = nullptr;
     int cur = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int graph_steps = 16;
@@ -297,6 +303,8 @@ int alloc_state(tds_sim* s) {
     if ((rc = dalloc(s, &s->packed_ids, N * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->st_d, 8 * N * sizeof(double)))) return rc;
     if ((rc = dalloc(s, &s->st_i, 2 * N * sizeof(int)))) return rc;
+    if ((rc = dalloc(s, &s->in_d, 6 * N * sizeof(double)))) return rc;
+    if ((rc = dalloc(s, &s->in_i, N * sizeof(int)))) return rc;
     CK(cudaMemset(s->count, 0, (size_t)s->M * sizeof(int)));
     CK(cudaMemset(s->tile_sum, 0, (size_t)2 * s->n_tiles * sizeof(int)));
     CK(cudaMemset(s->phi_acc, 0, (size_t)s->R * tdsk::kPhiCopies * 6 * sizeof(unsigned long long)));
@@ -498,8 +506,10 @@ int run_steps(tds_sim* s, int n, const double* noise_host, bool sync = true) {
     return TDS_OK;
 }
 
+// Input: host -> input staging on the upload stream, then the load on the compute stream. The
+// upload waits until the previous load has consumed the staging.
 template <typename real>
-int load_state(tds_sim* s, const tds_state_view* in) {
+int load_state(tds_sim* s, const tds_state_view* in, bool sync) {
     const size_t N = (size_t)s->N;
     if (!in || !in->uv || !in->theta) return fail(s, TDS_ERR_ARG, "set_state needs uv and theta");
     if (in->face) {
@@ -507,14 +517,17 @@ int load_state(tds_sim* s, const tds_state_view* in) {
         for (size_t i = 0; i < N; ++i) fmax = std::max(fmax, in->face[i]);
         if (fmax >= s->mesh->t.F) return fail(s, TDS_ERR_ARG, "set_state: face index out of range");
     }
-    double* d_uv = s->st_d;
-    double* d_th = s->st_d + 2 * N;
-    double* d_r3 = s->st_d + 3 * N;
-    int* d_face = s->st_i;
-    CK(cudaMemcpyAsync(d_uv, in->uv, 2 * N * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-    CK(cudaMemcpyAsync(d_th, in->theta, N * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-    if (in->face) CK(cudaMemcpyAsync(d_face, in->face, N * sizeof(int), cudaMemcpyHostToDevice, s->stream));
-    if (in->r3d) CK(cudaMemcpyAsync(d_r3, in->r3d, 3 * N * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    double* d_uv = s->in_d;
+    double* d_th = s->in_d + 2 * N;
+    double* d_r3 = s->in_d + 3 * N;
+    int* d_face = s->in_i;
+    CK(cudaStreamWaitEvent(s->up, s->ev_in_free, 0));
+    CK(cudaMemcpyAsync(d_uv, in->uv, 2 * N * sizeof(double), cudaMemcpyHostToDevice, s->up));
+    CK(cudaMemcpyAsync(d_th, in->theta, N * sizeof(double), cudaMemcpyHostToDevice, s->up));
+    if (in->face) CK(cudaMemcpyAsync(d_face, in->face, N * sizeof(int), cudaMemcpyHostToDevice, s->up));
+    if (in->r3d) CK(cudaMemcpyAsync(d_r3, in->r3d, 3 * N * sizeof(double), cudaMemcpyHostToDevice, s->up));
+    CK(cudaEventRecord(s->ev_in_ready, s->up));
+    CK(cudaStreamWaitEvent(s->stream, s->ev_in_ready, 0));
     s->cur = 0;
     const int nb = (s->N + 255) / 256;
     CK(cudaMemsetAsync(s->count, 0, (size_t)s->M * sizeof(int), s->stream));
@@ -527,12 +540,15 @@ int load_state(tds_sim* s, const tds_state_view* in) {
     tdsk::k_tile_sums<<<s->n_tiles, tdsk::kScanThreads, 0, s->stream>>>(s->count, s->M, s->tile_sum, s->n_tiles,
                                                                          s->d_step);
     CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaEventRecord(s->ev_in_free, s->stream));
+    if (sync) CK(cudaStreamSynchronize(s->stream));
     return TDS_OK;
 }
 
+// Output: gather into the output staging on the compute stream, then device -> host on the
+// download stream. The gather waits until the previous download has left the staging.
 template <typename real>
-int save_state(tds_sim* s, tds_state_view* out) {
+int save_state(tds_sim* s, tds_state_view* out, bool sync) {
     const size_t N = (size_t)s->N;
     double* d_uv = s->st_d;
     double* d_th = s->st_d + 2 * N;
@@ -542,18 +558,39 @@ int save_state(tds_sim* s, tds_state_view* out) {
     int* d_cnt = s->st_i + N;
     const int c = s->cur;
     const int nb = (s->N + 255) / 256;
+    CK(cudaStreamWaitEvent(s->stream, s->ev_out_free, 0));
     tdsk::k_gather_state<real><<<nb, 256, 0, s->stream>>>(
         (const R4<real>*)s->pos[c], (const R4<real>*)s->pol[c], (const R2<real>*)s->uv[c], s->ids[c],
         (const R2<real>*)s->vel[c], s->cnt[c], (const RepParams<real>*)s->reps, s->local_bits, d_uv, d_th, d_face, d_r3,
         d_vel, d_cnt, s->N);
     CK(cudaGetLastError());
-    if (out->uv) CK(cudaMemcpyAsync(out->uv, d_uv, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-    if (out->theta) CK(cudaMemcpyAsync(out->theta, d_th, N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-    if (out->face) CK(cudaMemcpyAsync(out->face, d_face, N * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-    if (out->r3d) CK(cudaMemcpyAsync(out->r3d, d_r3, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-    if (out->vel_uv) CK(cudaMemcpyAsync(out->vel_uv, d_vel, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-    if (out->nbr_count) CK(cudaMemcpyAsync(out->nbr_count, d_cnt, N * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaEventRecord(s->ev_out_ready, s->stream));
+    CK(cudaStreamWaitEvent(s->down, s->ev_out_ready, 0));
+    cudaStream_t d = s->down;
+    if (out->uv) CK(cudaMemcpyAsync(out->uv, d_uv, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, d));
+    if (out->theta) CK(cudaMemcpyAsync(out->theta, d_th, N * sizeof(double), cudaMemcpyDeviceToHost, d));
+    if (out->face) CK(cudaMemcpyAsync(out->face, d_face, N * sizeof(int), cudaMemcpyDeviceToHost, d));
+    if (out->r3d) CK(cudaMemcpyAsync(out->r3d, d_r3, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, d));
+    if (out->vel_uv) CK(cudaMemcpyAsync(out->vel_uv, d_vel, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, d));
+    if (out->nbr_count) CK(cudaMemcpyAsync(out->nbr_count, d_cnt, N * sizeof(int), cudaMemcpyDeviceToHost, d));
+    CK(cudaEventRecord(s->ev_out_free, d));
+    if (sync) CK(cudaStreamSynchronize(d));
+    return TDS_OK;
+}
+
+// Waits for every stream of the handle; a non-zero device status word is an error.
+int sync_all(tds_sim* s) {
+    CK(cudaStreamSynchronize(s->up));
     CK(cudaStreamSynchronize(s->stream));
+    CK(cudaStreamSynchronize(s->down));
+    int st = 0;
+    CK(cudaMemcpy(&st, s->status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st) {
+        char buf[224];
+        std::snprintf(buf, sizeof buf, "device status 0x%x after step %lld (1 non-finite, 2 wrap limit, 4 locate fallback, "
+                      "16 particle outside the surface cells)", st, s->step);
+        return fail(s, TDS_ERR_STATE, buf);
+    }
     return TDS_OK;
 }
 
@@ -671,7 +708,17 @@ int create_impl(const tds_mesh* mesh, int R, const int* n, const tds_params* prm
     s->N = (int)total;
     s->local_bits = R == 1 ? 31 : std::max(1, ceil_log2(nmax));
     if (R > 1 && ceil_log2(R) + s->local_bits > 31) return TDS_ERR_LIMIT;
-    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return TDS_ERR_CUDA;
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->up, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->down, cudaStreamNonBlocking) != cudaSuccess) {
+        tds_destroy(s.release());
+        return TDS_ERR_CUDA;
+    }
+    for (cudaEvent_t* e : {&s->ev_in_ready, &s->ev_in_free, &s->ev_out_ready, &s->ev_out_free})
+        if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) {
+            tds_destroy(s.release());
+            return TDS_ERR_CUDA;
+        }
     tds_sim* sp = s.get();
     int rc = precision == 32 ? upload_tables<float>(sp) : upload_tables<double>(sp);
     if (!rc) rc = precision == 32 ? alloc_state<float>(sp) : alloc_state<double>(sp);
@@ -828,12 +875,27 @@ int tds_update(tds_sim* s, tds_state_view* out) {
 
 int tds_set_state(tds_sim* s, const tds_state_view* in) {
     if (!s) return TDS_ERR_ARG;
-    return s->precision == 32 ? load_state<float>(s, in) : load_state<double>(s, in);
+    return s->precision == 32 ? load_state<float>(s, in, true) : load_state<double>(s, in, true);
 }
 
 int tds_get_state(tds_sim* s, tds_state_view* out) {
     if (!s || !out) return TDS_ERR_ARG;
-    return s->precision == 32 ? save_state<float>(s, out) : save_state<double>(s, out);
+    return s->precision == 32 ? save_state<float>(s, out, true) : save_state<double>(s, out, true);
+}
+
+int tds_set_state_async(tds_sim* s, const tds_state_view* in) {
+    if (!s) return TDS_ERR_ARG;
+    return s->precision == 32 ? load_state<float>(s, in, false) : load_state<double>(s, in, false);
+}
+
+int tds_get_state_async(tds_sim* s, tds_state_view* out) {
+    if (!s || !out) return TDS_ERR_ARG;
+    return s->precision == 32 ? save_state<float>(s, out, false) : save_state<double>(s, out, false);
+}
+
+int tds_sync(tds_sim* s) {
+    if (!s) return TDS_ERR_ARG;
+    return sync_all(s);
 }
 
 int tds_get_state_noalloc(tds_sim* s, tds_state_view* out) {
@@ -901,14 +963,20 @@ const char* tds_last_error(const tds_sim* s) { return s ? s->err.c_str() : "null
 
 void tds_destroy(tds_sim* s) {
     if (!s) return;
+    if (s->up) cudaStreamSynchronize(s->up);
     if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->down) cudaStreamSynchronize(s->down);
     collect_times(s);
     for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
     free_graphs(s);
     for (void* p : s->allocs) cudaFree(p);
     if (s->series) cudaFree(s->series);
     if (s->noise) cudaFree(s->noise);
+    for (cudaEvent_t e : {s->ev_in_ready, s->ev_in_free, s->ev_out_ready, s->ev_out_free})
+        if (e) cudaEventDestroy(e);
     if (s->stream) cudaStreamDestroy(s->stream);
+    if (s->up) cudaStreamDestroy(s->up);
+    if (s->down) cudaStreamDestroy(s->down);
     delete s;
 }
 

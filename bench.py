@@ -8,8 +8,9 @@ r_max = 2.4 R), eta = 0.3, dt = 0.01, FP32 state. Synthetic, seeded placement (n
 One bench step = one simulation step of the whole system (5 kernels). L2 is flushed (a 256 MB
 write, outside the timed window) before every timed step; each step is timed with CUDA events on
 the handle's stream. value = particle-steps/s over all ranks (max time over ranks).
-e2e = the same metric through the C-ABI with host buffers: set_state (H2D) + tds_step + get_state
-(D2H) per step, from/to pinned host memory.
+e2e = the same metric through the C-ABI with host buffers: set_state (H2D) + step + get_state (D2H)
+per step, from/to pinned host memory, enqueued with the pipelined calls so that the upload of step
+k+1 overlaps the download of step k (the synchronous-call figure is reported beside it).
 
 --impl reference times the CPU restatement of the path (oracle, FP64, all host threads) on the same
 workload; under torchrun only rank 0 runs it.
@@ -290,7 +291,11 @@ def run_gpu(args):
     pin_out = dict(uv=pinned((n, 2), torch.float64), theta=pinned((n,), torch.float64),
                    face=pinned((n,), torch.int32), r3d=pinned((n, 3), torch.float64),
                    vel_uv=pinned((n, 2), torch.float64), nbr=pinned((n,), torch.int32))
+    pin_out2 = {k: pinned(v.shape, torch.float64 if v.dtype == np.float64 else torch.int32) for k, v in pin_out.items()}
     e2e_steps = max(3, min(args.steps, 20))
+    h2d_bytes = int(sum(v.nbytes for v in pin_in.values()))
+    d2h_bytes = int(sum(v.nbytes for v in pin_out.values()))
+    # synchronous: each call returns when its transfer is done
     sim.set_state(**pin_in)
     sim.step(1)
     sim.get_state(pin_out)
@@ -300,11 +305,27 @@ def run_gpu(args):
         sim.set_state(**pin_in)
         sim.step(1)
         sim.get_state(pin_out)
+    sync_s = allreduce_max(time.perf_counter() - t0, world)
+    # pipelined: the same calls enqueued; step k+1's upload overlaps step k's download
+    # (host outputs double-buffered, as a caller consuming the results would)
+    sim.set_state_async(**pin_in)
+    sim.step_async(1)
+    sim.get_state_async(pin_out)
+    sim.sync()
+    barrier(world)
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        sim.set_state_async(**pin_in)
+        sim.step_async(1)
+        sim.get_state_async(pin_out if k % 2 == 0 else pin_out2)
+    sim.sync()
     e2e_s = allreduce_max(time.perf_counter() - t0, world)
     e2e = {"value": world * n * e2e_steps / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": int(sum(v.nbytes for v in pin_in.values())),
-           "d2h_bytes_per_step": int(sum(v.nbytes for v in pin_out.values())),
-           "path": "tds_set_state (pinned H2D) + tds_step + tds_get_state (pinned D2H)"}
+           "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
+           "path": "per step: tds_set_state_async (pinned H2D, upload stream) + tds_step_async + "
+                   "tds_get_state_async (pinned D2H, download stream); tds_sync after the last step",
+           "synchronous": {"value": world * n * e2e_steps / sync_s, "unit": UNIT,
+                           "path": "tds_set_state + tds_step + tds_get_state, each waiting"}}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

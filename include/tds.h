@@ -117,6 +117,19 @@ int tds_num_particles(const tds_sim* sim, int* n_total, int* n_replicas);
 /* Launches n_steps on the handle's stream and returns without waiting; the status word is
  * checked by the next tds_step / tds_get_status. For pipelined callers and device-timed loops. */
 int tds_step_async(tds_sim* sim, int n_steps);
+/* Pipelined state transfer (no counterpart in the reference, whose state never leaves host
+ * memory). Same results as tds_set_state / tds_get_state, but they only enqueue and return:
+ * uploads run on the handle's upload stream, downloads on its download stream, the load, the
+ * gather and the steps on its compute stream, ordered by events. The host link carries both
+ * directions at once, so in a loop set(k) -> step -> get(k) the upload of step k+1 overlaps the
+ * download of step k. Host arrays passed in must stay untouched (inputs) or unread (outputs)
+ * until tds_sync returns; pinned host memory makes the copies asynchronous. Input validation
+ * (face range) happens at the call. */
+int tds_set_state_async(tds_sim* sim, const tds_state_view* in);
+int tds_get_state_async(tds_sim* sim, tds_state_view* out);
+/* Waits for all work of the handle (transfers and steps); TDS_ERR_STATE if the device status
+ * word is non-zero. */
+int tds_sync(tds_sim* sim);
 /* Per-kernel CUDA-event timing of directly launched steps (graphs are not used while enabled).
  * tds_kernel_times returns, per kernel (0 scan, 1 scatter, 2 order, 3 step, 4 finalize), the
  * summed device time in ms and the launch count since timing was enabled (arrays of 5). */
