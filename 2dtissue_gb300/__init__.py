@@ -39,6 +39,20 @@ class _Params(C.Structure):
                                           "eta", "dt")] + [("force_mode", C.c_int), ("reserved", C.c_int)]
 
 
+class _AdjSpec(C.Structure):
+    _fields_ = [("n_steps", C.c_int), ("checkpoint_stride", C.c_int), ("r3d_target", C.c_void_p),
+                ("w_pos", C.c_double), ("phi_target", C.c_void_p), ("w_phi", C.c_double)]
+
+
+class _AdjResult(C.Structure):
+    _fields_ = [("loss", C.c_double), ("d_params", C.c_void_p), ("d_uv0", C.c_void_p), ("d_theta0", C.c_void_p),
+                ("checkpoint_stride", C.c_int)]
+
+
+# order of the parameter gradients returned by the adjoint
+GRAD_PARAMS = ("k_rep", "k_adh", "v0", "mu", "tau", "align", "eta")
+
+
 class _StateView(C.Structure):
     _fields_ = [("uv", C.c_void_p), ("theta", C.c_void_p), ("face", C.c_void_p), ("r3d", C.c_void_p),
                 ("vel_uv", C.c_void_p), ("nbr_count", C.c_void_p)]
@@ -80,6 +94,8 @@ def lib(build_if_missing=True):
     L.tds_set_state_async.argtypes = [VP, P(_StateView)]
     L.tds_get_state_async.argtypes = [VP, P(_StateView)]
     L.tds_sync.argtypes = [VP]
+    L.tds_set_params.argtypes = [VP, VP]
+    L.tds_adjoint_run.argtypes = [VP, P(_AdjSpec), P(_AdjResult)]
     L.tds_get_order_parameter.argtypes = [VP, VP, VP, I, P(I)]
     L.tds_get_step.argtypes = [VP, P(C.c_int64)]
     L.tds_get_status.argtypes = [VP, P(I)]
@@ -288,6 +304,29 @@ class Simulation:
             self._check(lib().tds_sync(self.h))
         finally:
             self._pending = []
+
+    def set_params(self, params):
+        """New model parameters (one Params, or one per replica); radius and r_max must not change."""
+        ps = list(params) if isinstance(params, (list, tuple)) else [params] * self.R
+        arr = (_Params * len(ps))(*[q.to_c() for q in ps])
+        self._check(lib().tds_set_params(self.h, C.cast(arr, C.c_void_p)))
+        self.params = ps
+
+    def adjoint(self, n_steps, r3d_target=None, w_pos=0.0, phi_target=None, w_phi=0.0, checkpoint_stride=0):
+        """Runs n_steps forward from the current state, then the hand-written reverse sweep.
+        Loss = w_pos * sum_r mean_i |r_T - r*|^2 + w_phi * sum_t sum_r (phi_t - phi*_t)^2.
+        Returns loss, d_params (R x 7, order GRAD_PARAMS), d_uv0 (N x 2), d_theta0 (N) and the
+        checkpoint stride used."""
+        N, R = self.N, self.R
+        tgt = None if r3d_target is None else np.ascontiguousarray(r3d_target, np.float64).reshape(N, 3)
+        phi = None if phi_target is None else np.ascontiguousarray(phi_target, np.float64).reshape(n_steps, R)
+        spec = _AdjSpec(int(n_steps), int(checkpoint_stride), _ptr(tgt), float(w_pos), _ptr(phi), float(w_phi))
+        dp = np.zeros((R, 8))
+        duv = np.zeros((N, 2))
+        dth = np.zeros(N)
+        res = _AdjResult(0.0, _ptr(dp), _ptr(duv), _ptr(dth), 0)
+        self._check(lib().tds_adjoint_run(self.h, C.byref(spec), C.byref(res)))
+        return dict(loss=res.loss, d_params=dp[:, :7], d_uv0=duv, d_theta0=dth, checkpoint_stride=res.checkpoint_stride)
 
     def get_state_noalloc(self, out=None):
         """Same as get_state, staged in the library's fixed device array (no device allocation;

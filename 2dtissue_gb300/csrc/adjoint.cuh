@@ -1,0 +1,385 @@
+// Reverse mode (adjoint) of the model step, with the neighbour sets, the face locations and the
+// seam-wrap sequences held at the values of the forward step.
+//
+// State per particle: chart position uv and polarity angle theta (the face is discrete). The 3D
+// position is r = A_f + J_f (uv - a_f) and the 3D polarity p = normalize(J_f (cos th, sin th)),
+// so the adjoint state is (ubar, vbar, thetabar) per particle, indexed by global particle index.
+//
+// One reverse step of step t is two launches over step t's sorted state:
+//   k_adj_a  per particle: recomputes the forward update (pair sums, velocity, polarity rotation,
+//            chart advance, seam wrap, location, map) and runs its reverse from the adjoint of the
+//            state after the step (plus the loss terms on the new positions and the order
+//            parameter) down to the adjoints of the pair sums F (force) and m (neighbour polarity)
+//            and the particle's own direct terms; parameter terms of v0, mu, tau, align, eta.
+//   k_adj_b  per particle k, over the same neighbours j (the relation is symmetric):
+//            rbar_k = sum_j K(r_k - r_j) (Fbar_k - Fbar_j),  pbar_k += sum_j mbar_j,
+//            K(x) = f'(d) e e^T + f(d)/d (I - e e^T) the Jacobian of one pair force, e = x/d;
+//            terms of k_rep, k_adh; then the adjoint of (uv, theta) before the step.
+// Gathering over neighbours instead of scattering keeps the sums free of atomics and in a fixed
+// order, so the adjoint is deterministic like the forward step.
+#pragma once
+#include "kernels.cuh"
+
+namespace tdsk {
+
+enum : int { G_KREP = 0, G_KADH = 1, G_V0 = 2, G_MU = 3, G_TAU = 4, G_ALIGN = 5, G_ETA = 6, kGPar = 8 };
+
+template <typename real>
+struct AdjArgs {
+    // step t's sorted state (k_order output) and cell starts
+    const R4<real>* pos;
+    const R4<real>* pol;
+    const R2<real>* uv;
+    const int* ids;
+    const int* key;
+    const int* start;
+    const uint4* desc;
+    const real* rec;
+    const int4* adj;
+    int G;
+    const int* bin_start;
+    const int* bin_faces;
+    const RepParams<real>* reps;
+    int local_bits;
+    real cx, cy, cz;
+    long long step;  // noise counter of step t
+    unsigned long long seed;
+    const real* noise;  // injected noise of step t by global index, or null
+    // loss terms of step t
+    const double* phisum;    // [R][6] order-parameter sums of step t (null: no order-parameter term)
+    const double* phibar;    // [R] dL/dphi_t
+    const double* r_target;  // [3N] by global index, last step only (null otherwise)
+    double w_pos;
+    // adjoint state
+    const real* lam_in;  // [3N] adjoint of (u, v, theta) after step t
+    real* lam_out;       // [3N] adjoint before step t
+    R4<real>* aF;        // [N] by slot: (Fbar, ubar_direct.x)
+    R4<real>* aM;        // [N] by slot: (mbar, ubar_direct.y)
+    R4<real>* aP;        // [N] by slot: (pbar_direct, 0)
+    double* gpar;        // [N][kGPar] by global index
+    int N;
+};
+
+// The 9 candidate runs of a particle's cell (slot ranges in the sorted state).
+template <typename real>
+__device__ __forceinline__ int candidate_runs(const RepParams<real>& rp, const uint4* desc, const int* start, int key,
+                                              int (&rs)[9], int (&rc)[9]) {
+    int total = 0;
+    const int id0 = key - rp.base;
+#pragma unroll
+    for (int r = 0; r < 9; ++r) rs[r] = 0, rc[r] = 0;
+    if (id0 < rp.C) {
+        const uint4* dp = desc + (size_t)rp.desc_off + (size_t)id0 * 3;
+        const uint4 d0 = dp[0], d1 = dp[1], d2 = dp[2];
+        const unsigned e[9] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w, d2.x};
+#pragma unroll
+        for (int r = 0; r < 9; ++r) {
+            const int first = (int)(e[r] >> 4), len = (int)(e[r] & 3u);
+            const int b0 = rp.base + first;
+            const int t0 = len ? start[b0] : 0;
+            const int t1 = len ? start[b0 + len] : 0;
+            rs[r] = t0;
+            rc[r] = t1 - t0;
+            total += t1 - t0;
+        }
+    }
+    return total;
+}
+
+// Visits the candidates in the forward step's order (runs 0..8, slots ascending).
+template <typename F>
+__device__ __forceinline__ void for_candidates(const int (&rs)[9], const int (&rc)[9], int total, F&& fn) {
+    int r = 0, t = rs[0], left = rc[0];
+    for (int k = 0; k < total; ++k) {
+        while (left == 0) {
+            ++r;
+            t = rs[r];
+            left = rc[r];
+        }
+        fn(t);
+        ++t;
+        --left;
+    }
+}
+
+template <typename real>
+__device__ __forceinline__ void cross(const real a[3], const real b[3], real o[3]) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+template <typename real>
+__device__ __forceinline__ real dot(const real a[3], const real b[3]) {
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+template <typename real>
+__global__ void __launch_bounds__(256) k_adj_a(const AdjArgs<real> a) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= a.N) return;
+    const R4<real> P = a.pos[q];
+    const R4<real> PL = a.pol[q];
+    const R2<real> U = a.uv[q];
+    const int id = a.ids[q];
+    const int rep = (int)((unsigned)id >> a.local_bits);
+    const unsigned local = (unsigned)id & ((1u << a.local_bits) - 1u);
+    const RepParams<real>& rp = a.reps[rep];
+    const int gid = rp.off + (int)local;
+    const int f = real_to_face(PL.w);
+    const real* g = a.rec + (size_t)f * kRec;
+
+    // ---- forward recompute (the arithmetic of k_step) ----
+    int rs[9], rc[9];
+    const int total = candidate_runs(rp, a.desc, a.start, a.key[q], rs, rc);
+    real acc[6] = {0, 0, 0, 0, 0, 0};
+    int cnt = 0;
+    for_candidates(rs, rc, total, [&](int t) { pair_term(rp, P, a.pos[t], a.pol, t, t == q, acc, cnt); });
+    const real p[3] = {PL.x, PL.y, PL.z};
+    const real F[3] = {acc[0], acc[1], acc[2]};
+    const real m[3] = {acc[3], acc[4], acc[5]};
+    real n[3], Jp[6];
+    face_frame(g, n, Jp);
+    const real Fn = dot(F, n);
+    const real FT[3] = {F[0] - Fn * n[0], F[1] - Fn * n[1], F[2] - Fn * n[2]};
+    real v[3], sp = (real)0, FTn = (real)0;
+    if (rp.force_mode == 0) {
+        for (int k = 0; k < 3; ++k) v[k] = rp.v0 * p[k] + rp.mu * FT[k];
+    } else {
+        const real t2 = dot(FT, FT);
+        FTn = t2 > (real)0 ? t2 * d_rsqrt(t2) : (real)0;
+        sp = rp.v0 + FTn;
+        for (int k = 0; k < 3; ++k) v[k] = sp * p[k];
+    }
+    const real vn2 = dot(v, v), mn2 = dot(m, m);
+    const real ivn = vn2 > (real)0 ? d_rsqrt(vn2) : (real)0;
+    const real imn = mn2 > (real)0 ? d_rsqrt(mn2) : (real)0;
+    real pxv[3], pxm[3];
+    cross(p, v, pxv);
+    cross(p, m, pxm);
+    const real A1 = dot(pxv, n), B1 = dot(pxm, n);
+    const real omega = A1 * ivn * rp.inv_tau + rp.align * B1 * imn;
+    real xi, u01 = (real)0.5;
+    if (a.noise) {
+        xi = a.noise[gid];
+    } else {
+        const unsigned bits = tdsr::noise_bits24(a.seed, a.step, local, (unsigned)rep);
+        u01 = (real)bits * (real)(1.0 / 16777216.0);
+        xi = rp.eta * (u01 - (real)0.5);
+    }
+    const real delta = rp.dt * omega + xi;
+    real sd, cd;
+    d_sincos(delta, &sd, &cd);
+    real np[3];
+    cross(n, p, np);
+    const real p2[3] = {cd * p[0] + sd * np[0], cd * p[1] + sd * np[1], cd * p[2] + sd * np[2]};
+    const real w0 = Jp[0] * p2[0] + Jp[1] * p2[1] + Jp[2] * p2[2];
+    const real w1 = Jp[3] * p2[0] + Jp[4] * p2[1] + Jp[5] * p2[2];
+    const real vu = Jp[0] * v[0] + Jp[1] * v[1] + Jp[2] * v[2];
+    const real vv = Jp[3] * v[0] + Jp[4] * v[1] + Jp[5] * v[2];
+    const real u2 = U.x + rp.dt * vu, v2 = U.y + rp.dt * vv;
+    real ex = u2, ey = v2, tvu = vu, tvv = vv, tw0 = w0, tw1 = w1;
+    int nw = 0;
+    seam_wrap(U.x, U.y, ex, ey, tvu, tvv, tw0, tw1, nw);
+    // linear part of the composed gluing maps: the same wrap applied to the unit vectors
+    real R00 = 1, R10 = 0, R01 = 0, R11 = 1;
+    if (nw > 0) {
+        real ex2 = u2, ey2 = v2;
+        int nw2 = 0;
+        seam_wrap(U.x, U.y, ex2, ey2, R00, R10, R01, R11, nw2);
+    }
+    int mode = 0;
+    const int f2 = locate(a.rec, a.adj, a.G, a.bin_start, a.bin_faces, ex, ey, f, mode);
+    const real* h = a.rec + (size_t)f2 * kRec;
+    real r2[3];
+    face_map(h, ex, ey, r2[0], r2[1], r2[2]);
+
+    // ---- reverse ----
+    real ub3x = a.lam_in[3 * (size_t)gid], ub3y = a.lam_in[3 * (size_t)gid + 1];
+    const real thb2 = a.lam_in[3 * (size_t)gid + 2];
+    real rb2[3] = {0, 0, 0}, vb[3] = {0, 0, 0};
+    if (a.r_target) {
+        const real s = (real)(2.0 * a.w_pos) * (real)rp.inv_n;
+        for (int k = 0; k < 3; ++k) rb2[k] += s * (r2[k] - (real)a.r_target[3 * (size_t)gid + k]);
+    }
+    if (a.phisum) {
+        // phi = |S| / N_r with S = sum_i normalize((r2_i - c) x v_i)
+        const double S0 = a.phisum[rep * 6], S1 = a.phisum[rep * 6 + 1], S2 = a.phisum[rep * 6 + 2];
+        const double Sn = sqrt(S0 * S0 + S1 * S1 + S2 * S2);
+        const real rc3[3] = {r2[0] - a.cx, r2[1] - a.cy, r2[2] - a.cz};
+        real L[3];
+        cross(rc3, v, L);
+        const real Ln2 = dot(L, L);
+        if (Sn > 0 && Ln2 > (real)0) {
+            const double c = a.phibar[rep] * rp.inv_n / Sn;
+            const real Sb[3] = {(real)(c * S0), (real)(c * S1), (real)(c * S2)};
+            const real iL = d_rsqrt(Ln2);
+            const real ell[3] = {L[0] * iL, L[1] * iL, L[2] * iL};
+            const real se = dot(Sb, ell);
+            const real Lb[3] = {(Sb[0] - se * ell[0]) * iL, (Sb[1] - se * ell[1]) * iL, (Sb[2] - se * ell[2]) * iL};
+            real t1[3], t2[3];
+            cross(v, Lb, t1);    // rc3bar = v x Lbar
+            cross(Lb, rc3, t2);  // vbar  += Lbar x rc
+            for (int k = 0; k < 3; ++k) rb2[k] += t1[k], vb[k] += t2[k];
+        }
+    }
+    // r2 = A' + J' (uv3 - a')
+    ub3x += h[8] * rb2[0] + h[9] * rb2[1] + h[10] * rb2[2];
+    ub3y += h[11] * rb2[0] + h[12] * rb2[1] + h[13] * rb2[2];
+    // uv3 = R uv2 + t
+    const real ub2x = R00 * ub3x + R10 * ub3y, ub2y = R01 * ub3x + R11 * ub3y;
+    // uv2 = uv + dt (Jp v)
+    const real velbx = rp.dt * ub2x, velby = rp.dt * ub2y;
+    for (int k = 0; k < 3; ++k) vb[k] += Jp[k] * velbx + Jp[3 + k] * velby;
+    // theta2 = atan2(w1, w0) + const (the gluing rotations only add constants)
+    const real iw2 = (real)1 / (w0 * w0 + w1 * w1);
+    const real wb0 = -w1 * iw2 * thb2, wb1 = w0 * iw2 * thb2;
+    // w = Jp p2
+    real p2b[3];
+    for (int k = 0; k < 3; ++k) p2b[k] = Jp[k] * wb0 + Jp[3 + k] * wb1;
+    // p2 = cos(delta) p + sin(delta) (n x p)
+    const real deltab = p2b[0] * (cd * np[0] - sd * p[0]) + p2b[1] * (cd * np[1] - sd * p[1]) +
+                        p2b[2] * (cd * np[2] - sd * p[2]);
+    real pb[3], p2bxn[3];
+    cross(p2b, n, p2bxn);
+    for (int k = 0; k < 3; ++k) pb[k] = cd * p2b[k] + sd * p2bxn[k];
+    // delta = dt omega + eta (u - 1/2)
+    const real omegab = rp.dt * deltab;
+    double gv0 = 0, gmu = 0, gtau = 0, galign = 0, geta = 0;
+    if (!a.noise) geta = (double)(deltab * (u01 - (real)0.5));
+    real mb[3] = {0, 0, 0};
+    real nxp[3];
+    cross(n, p, nxp);
+    if (vn2 > (real)0) {
+        // omega_1 = A1 / (|v| tau), A1 = p . (v x n)
+        const real A1b = omegab * ivn * rp.inv_tau;
+        const real vnb = -A1 * ivn * ivn * rp.inv_tau * omegab;
+        gtau += (double)(-A1 * ivn * rp.inv_tau * rp.inv_tau * omegab);
+        real vxn[3];
+        cross(v, n, vxn);
+        for (int k = 0; k < 3; ++k) pb[k] += A1b * vxn[k], vb[k] += A1b * nxp[k] + vnb * v[k] * ivn;
+    }
+    if (mn2 > (real)0) {
+        // omega_2 = align B1 / |m|, B1 = p . (m x n)
+        const real B1b = rp.align * omegab * imn;
+        const real mnb = -rp.align * B1 * imn * imn * omegab;
+        galign += (double)(B1 * imn * omegab);
+        real mxn[3];
+        cross(m, n, mxn);
+        for (int k = 0; k < 3; ++k) pb[k] += B1b * mxn[k], mb[k] += B1b * nxp[k] + mnb * m[k] * imn;
+    }
+    real FTb[3];
+    if (rp.force_mode == 0) {
+        // v = v0 p + mu FT
+        gv0 += (double)dot(vb, p);
+        gmu += (double)dot(vb, FT);
+        for (int k = 0; k < 3; ++k) pb[k] += rp.v0 * vb[k], FTb[k] = rp.mu * vb[k];
+    } else {
+        // v = (v0 + |FT|) p
+        const real spb = dot(vb, p);
+        gv0 += (double)spb;
+        const real s = FTn > (real)0 ? spb / FTn : (real)0;
+        for (int k = 0; k < 3; ++k) pb[k] += sp * vb[k], FTb[k] = s * FT[k];
+    }
+    // FT = F - (F . n) n
+    const real Fbn = dot(FTb, n);
+    R4<real> oF, oM, oP;
+    oF.x = FTb[0] - Fbn * n[0], oF.y = FTb[1] - Fbn * n[1], oF.z = FTb[2] - Fbn * n[2], oF.w = ub2x;
+    oM.x = mb[0], oM.y = mb[1], oM.z = mb[2], oM.w = ub2y;
+    oP.x = pb[0], oP.y = pb[1], oP.z = pb[2], oP.w = (real)0;
+    a.aF[q] = oF;
+    a.aM[q] = oM;
+    a.aP[q] = oP;
+    double* gp = a.gpar + (size_t)gid * kGPar;
+    gp[G_V0] += gv0;
+    gp[G_MU] += gmu;
+    gp[G_TAU] += gtau;
+    gp[G_ALIGN] += galign;
+    gp[G_ETA] += geta;
+}
+
+template <typename real>
+__global__ void __launch_bounds__(256) k_adj_b(const AdjArgs<real> a) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= a.N) return;
+    const R4<real> P = a.pos[q];
+    const R4<real> PL = a.pol[q];
+    const int id = a.ids[q];
+    const int rep = (int)((unsigned)id >> a.local_bits);
+    const unsigned local = (unsigned)id & ((1u << a.local_bits) - 1u);
+    const RepParams<real>& rp = a.reps[rep];
+    const int gid = rp.off + (int)local;
+    const int f = real_to_face(PL.w);
+    const real* g = a.rec + (size_t)f * kRec;
+    const R4<real> myF = a.aF[q], myM = a.aM[q], myP = a.aP[q];
+
+    int rs[9], rc[9];
+    const int total = candidate_runs(rp, a.desc, a.start, a.key[q], rs, rc);
+    real rb[3] = {0, 0, 0}, msum[3] = {0, 0, 0};
+    double gk = 0, gkadh = 0;
+    const real inv_w = rp.inv_adh_w;
+    for_candidates(rs, rc, total, [&](int t) {
+        const R4<real> Q = a.pos[t];
+        const real dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
+        const real d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 < rp.r_max2 && t != q) {
+            const R4<real> Fj = a.aF[t], Mj = a.aM[t];
+            msum[0] += Mj.x, msum[1] += Mj.y, msum[2] += Mj.z;
+            if (d2 > (real)0) {
+                const real rd = d_rsqrt(d2);
+                const real d = d2 * rd;
+                const bool rep_branch = d < rp.twoR;
+                const real fm = rep_branch ? rp.k * (rp.twoR - d) * rp.inv_twoR : -(rp.adh_scale * (d - rp.twoR));
+                const real fp = rep_branch ? -rp.k * rp.inv_twoR : -rp.adh_scale;
+                const real e[3] = {dx * rd, dy * rd, dz * rd};
+                const real D[3] = {myF.x - Fj.x, myF.y - Fj.y, myF.z - Fj.z};
+                const real eD = dot(e, D);
+                const real fd = fm * rd;
+                for (int k = 0; k < 3; ++k) rb[k] += fd * D[k] + (fp - fd) * eD * e[k];
+                const real Fe = myF.x * e[0] + myF.y * e[1] + myF.z * e[2];
+                if (rep_branch)
+                    gk += (double)(Fe * (rp.twoR - d) * rp.inv_twoR);
+                else
+                    gkadh += (double)(-Fe * (d - rp.twoR) * inv_w);
+            }
+        }
+    });
+    // r = A + J (uv - a)
+    const real ubx = myF.w + g[8] * rb[0] + g[9] * rb[1] + g[10] * rb[2];
+    const real uby = myM.w + g[11] * rb[0] + g[12] * rb[1] + g[13] * rb[2];
+    // p = normalize(J (cos th, sin th))
+    const real pbt[3] = {myP.x + msum[0], myP.y + msum[1], myP.z + msum[2]};
+    real sn, cs;
+    d_sincos(P.w, &sn, &cs);
+    const real qv[3] = {g[8] * cs + g[11] * sn, g[9] * cs + g[12] * sn, g[10] * cs + g[13] * sn};
+    const real iq = d_rsqrt(dot(qv, qv));
+    const real pp[3] = {qv[0] * iq, qv[1] * iq, qv[2] * iq};
+    const real pq = dot(pbt, pp);
+    const real qb[3] = {(pbt[0] - pq * pp[0]) * iq, (pbt[1] - pq * pp[1]) * iq, (pbt[2] - pq * pp[2]) * iq};
+    const real cb0 = g[8] * qb[0] + g[9] * qb[1] + g[10] * qb[2];
+    const real cb1 = g[11] * qb[0] + g[12] * qb[1] + g[13] * qb[2];
+    a.lam_out[3 * (size_t)gid] = ubx;
+    a.lam_out[3 * (size_t)gid + 1] = uby;
+    a.lam_out[3 * (size_t)gid + 2] = -sn * cb0 + cs * cb1;
+    double* gp = a.gpar + (size_t)gid * kGPar;
+    gp[G_KREP] += gk;
+    gp[G_KADH] += gkadh;
+}
+
+// Per-replica sums of the per-particle parameter terms, in a fixed order (one block per replica).
+__global__ void k_adj_reduce(const double* gpar, const int* off, const int* cnt, double* out) {
+    __shared__ double s[256][kGPar];
+    const int r = blockIdx.x;
+    double acc[kGPar] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = off[r] + threadIdx.x; i < off[r] + cnt[r]; i += 256)
+        for (int k = 0; k < kGPar; ++k) acc[k] += gpar[(size_t)i * kGPar + k];
+    for (int k = 0; k < kGPar; ++k) s[threadIdx.x][k] = acc[k];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w)
+            for (int k = 0; k < kGPar; ++k) s[threadIdx.x][k] += s[threadIdx.x + w][k];
+        __syncthreads();
+    }
+    if (threadIdx.x < kGPar) out[(size_t)r * kGPar + threadIdx.x] = s[0][threadIdx.x];
+}
+
+}  // namespace tdsk

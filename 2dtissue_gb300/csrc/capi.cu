@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/tds.h"
+#include "adjoint.cuh"
 #include "geometry.hpp"
 #include "kernels.cuh"
 #include "mesh.hpp"
@@ -75,6 +76,7 @@ struct tds_sim {
     int* bin_faces = nullptr;
     int G = 1;
     void* reps = nullptr;
+    std::vector<unsigned char> reps_host;  // host copy of the replica table
     long long M = 0;
     int n_tiles = 0;
     void* pos[2] = {nullptr, nullptr};
@@ -145,6 +147,24 @@ void free_graphs(tds_sim* s) {
             cudaGraphExecDestroy(g);
             g = nullptr;
         }
+}
+
+// Model parameters of one replica into its device record (the cell-level fields stay).
+template <typename real>
+void fill_params(RepParams<real>& q, const tds_params& p) {
+    q.twoR = (real)(2 * p.radius);
+    q.inv_twoR = (real)(1.0 / (2 * p.radius));
+    q.k = (real)p.k_rep;
+    q.adh_scale = (real)(p.k_adh / (p.r_max - 2 * p.radius));
+    q.inv_adh_w = (real)(1.0 / (p.r_max - 2 * p.radius));
+    q.r_max2 = (real)(p.r_max * p.r_max);
+    q.v0 = (real)p.v0;
+    q.mu = (real)p.mu;
+    q.inv_tau = (real)(1.0 / p.tau);
+    q.align = (real)p.align;
+    q.eta = (real)p.eta;
+    q.dt = (real)p.dt;
+    q.force_mode = p.force_mode;
 }
 
 template <typename real>
@@ -245,22 +265,11 @@ int upload_tables(tds_sim* s) {
         std::memset(&q, 0, sizeof q);
         const Level& lv = levels[s->level_of[r]];
         const double h = lv.L.h;
-        q.twoR = (real)(2 * p.radius);
-        q.inv_twoR = (real)(1.0 / (2 * p.radius));
-        q.k = (real)p.k_rep;
-        q.adh_scale = (real)(p.k_adh / (p.r_max - 2 * p.radius));
-        q.r_max2 = (real)(p.r_max * p.r_max);
-        q.v0 = (real)p.v0;
-        q.mu = (real)p.mu;
-        q.inv_tau = (real)(1.0 / p.tau);
-        q.align = (real)p.align;
-        q.eta = (real)p.eta;
-        q.dt = (real)p.dt;
+        fill_params(q, p);
         q.inv_h = (real)(1.0 / h);
         // order parameter: warp sums (|.| <= 32) in 64-bit fixed point, N_r terms per replica
         q.phiscale = std::ldexp(1.0, 62 - ceil_log2((long long)s->n_rep[r] + 1));
         q.inv_n = 1.0 / std::max(1, s->n_rep[r]);
-        q.force_mode = p.force_mode;
         q.ox = (real)lv.origin[0], q.oy = (real)lv.origin[1], q.oz = (real)lv.origin[2];
         q.base = (int)base;
         q.C = lv.L.C;
@@ -275,6 +284,7 @@ int upload_tables(tds_sim* s) {
     s->M = base;
     if ((rc = dalloc(s, (RepParams<real>**)&s->reps, rp.size() * sizeof(RepParams<real>)))) return rc;
     CK(cudaMemcpy(s->reps, rp.data(), rp.size() * sizeof(RepParams<real>), cudaMemcpyHostToDevice));
+    s->reps_host.assign((const unsigned char*)rp.data(), (const unsigned char*)(rp.data() + rp.size()));
     return TDS_OK;
 }
 
@@ -385,33 +395,57 @@ void collect_times(tds_sim* s) {
     s->ev_pending.clear();
 }
 
+// What a step can leave behind for the adjoint: its sorted state and cell starts (copied right
+// after k_order) and its order-parameter sums.
+struct StepStore {
+    void* pos = nullptr;
+    void* pol = nullptr;
+    void* uv = nullptr;
+    int* ids = nullptr;
+    int* key = nullptr;
+    int* start = nullptr;
+};
+struct StepHooks {
+    const StepStore* store = nullptr;
+    double* phisum = nullptr;
+    long long phisum_base = 0, phisum_cap = 0;
+};
+
 // Buffer roles: index 0 = step output (and set_state target), index 1 = sorted copy.
 template <typename real>
-void launch_one_step(tds_sim* s, const real* noise) {
+void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullptr) {
     const int c = 1, o = 0;
     cudaStream_t st = s->stream;
+    // the sorted copy and the cell starts of this step go to the handle's buffer 1, or straight
+    // into an adjoint store slot
+    const StepStore* x = hk ? hk->store : nullptr;
+    R4<real>* cpos = (R4<real>*)(x ? x->pos : s->pos[c]);
+    R4<real>* cpol = (R4<real>*)(x ? x->pol : s->pol[c]);
+    R2<real>* cuv = (R2<real>*)(x ? x->uv : s->uv[c]);
+    int* cids = x ? x->ids : s->ids[c];
+    int* ckey = x ? x->key : s->key[c];
+    int* start = x ? x->start : s->start;
     {
         KernelTimer kt(s, 0);
-        tdsk::k_scan<<<s->n_tiles, tdsk::kScanThreads, 0, st>>>(s->count, s->start, s->M, s->tile_sum, s->n_tiles,
+        tdsk::k_scan<<<s->n_tiles, tdsk::kScanThreads, 0, st>>>(s->count, start, s->M, s->tile_sum, s->n_tiles,
                                                                  s->d_step);
     }
     const int nb = (s->N + 255) / 256;
     {
         KernelTimer kt(s, 1);
-        tdsk::k_scatter<<<nb, 256, 0, st>>>(s->key[o], s->count, s->start, s->tmp, s->N, s->d_step);
+        tdsk::k_scatter<<<nb, 256, 0, st>>>(s->key[o], s->count, start, s->tmp, s->N, s->d_step);
     }
     {
         KernelTimer kt(s, 2);
-        tdsk::k_order<real><<<nb, 256, 0, st>>>(s->tmp, s->key[o], s->ids[o], s->start, (const R4<real>*)s->pos[o],
-                                                 (const R4<real>*)s->pol[o], (const R2<real>*)s->uv[o],
-                                                 (R4<real>*)s->pos[c], (R4<real>*)s->pol[c], (R2<real>*)s->uv[c],
-                                                 s->ids[c], s->key[c], s->N);
+        tdsk::k_order<real><<<nb, 256, 0, st>>>(s->tmp, s->key[o], s->ids[o], start, (const R4<real>*)s->pos[o],
+                                                 (const R4<real>*)s->pol[o], (const R2<real>*)s->uv[o], cpos, cpol,
+                                                 cuv, cids, ckey, s->N);
     }
     tdsk::StepArgs<real> a;
-    a.pos = (const R4<real>*)s->pos[c];
-    a.pol = (const R4<real>*)s->pol[c];
-    a.uv = (const R2<real>*)s->uv[c];
-    a.ids = s->ids[c];
+    a.pos = cpos;
+    a.pol = cpol;
+    a.uv = cuv;
+    a.ids = cids;
     a.pos_o = (R4<real>*)s->pos[o];
     a.pol_o = (R4<real>*)s->pol[o];
     a.uv_o = (R2<real>*)s->uv[o];
@@ -419,9 +453,9 @@ void launch_one_step(tds_sim* s, const real* noise) {
     a.vel_o = (R2<real>*)s->vel[o];
     a.cnt_o = s->cnt[o];
     a.key_o = s->key[o];
-    a.key_in = s->key[c];
+    a.key_in = ckey;
     a.desc = s->desc;
-    a.start = s->start;
+    a.start = start;
     a.count = s->count;
     a.tile_sum = s->tile_sum;
     a.n_tiles = s->n_tiles;
@@ -449,7 +483,8 @@ void launch_one_step(tds_sim* s, const real* noise) {
     {
         KernelTimer kt(s, 4);
         tdsk::k_finalize<real><<<s->R, 128, 0, st>>>(
-            s->phi_acc, (const RepParams<real>*)s->reps, s->R, s->series, 0, s->series_cap, s->d_step);
+            s->phi_acc, (const RepParams<real>*)s->reps, s->R, s->series, 0, s->series_cap, s->d_step,
+            hk ? hk->phisum : nullptr, hk ? hk->phisum_base : 0, hk ? hk->phisum_cap : 0);
     }
 }
 
@@ -591,6 +626,264 @@ int sync_all(tds_sim* s) {
                       "16 particle outside the surface cells)", st, s->step);
         return fail(s, TDS_ERR_STATE, buf);
     }
+    return TDS_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Adjoint run (tds_adjoint_run): forward with checkpoints, loss, reverse sweep
+// ---------------------------------------------------------------------------------------------
+// Device memory of one adjoint run, released when it returns.
+struct Arena {
+    std::vector<void*> p;
+    ~Arena() {
+        for (void* q : p) cudaFree(q);
+    }
+    template <typename T>
+    T* get(size_t n) {
+        void* q = nullptr;
+        if (cudaMalloc(&q, std::max<size_t>(n * sizeof(T), 16)) != cudaSuccess) return nullptr;
+        p.push_back(q);
+        return (T*)q;
+    }
+};
+
+// The input state of a step: buffer 0, the cell counts, the per-tile counts and the step counter.
+template <typename real>
+struct Snapshot {
+    R4<real>* pos = nullptr;
+    R4<real>* pol = nullptr;
+    R2<real>* uv = nullptr;
+    int* ids = nullptr;
+    int* key = nullptr;
+    int* count = nullptr;
+    int* tile_sum = nullptr;
+    long long* d_step = nullptr;
+    bool alloc(Arena& A, size_t N, size_t M, int n_tiles) {
+        pos = A.get<R4<real>>(N), pol = A.get<R4<real>>(N), uv = A.get<R2<real>>(N);
+        ids = A.get<int>(N), key = A.get<int>(N), count = A.get<int>(M), tile_sum = A.get<int>(2 * (size_t)n_tiles);
+        d_step = A.get<long long>(1);
+        return pos && pol && uv && ids && key && count && tile_sum && d_step;
+    }
+};
+
+template <typename real>
+void snapshot_copy(tds_sim* s, const Snapshot<real>& x, bool take) {
+    const size_t N = (size_t)s->N;
+    auto cp = [&](void* snap, void* live, size_t bytes) {
+        if (take)
+            cudaMemcpyAsync(snap, live, bytes, cudaMemcpyDeviceToDevice, s->stream);
+        else
+            cudaMemcpyAsync(live, snap, bytes, cudaMemcpyDeviceToDevice, s->stream);
+    };
+    cp(x.pos, s->pos[0], N * sizeof(R4<real>));
+    cp(x.pol, s->pol[0], N * sizeof(R4<real>));
+    cp(x.uv, s->uv[0], N * sizeof(R2<real>));
+    cp(x.ids, s->ids[0], N * sizeof(int));
+    cp(x.key, s->key[0], N * sizeof(int));
+    cp(x.count, s->count, (size_t)s->M * sizeof(int));
+    cp(x.tile_sum, s->tile_sum, 2 * (size_t)s->n_tiles * sizeof(int));
+    cp(x.d_step, s->d_step, sizeof(long long));
+}
+
+template <typename real>
+int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp, tds_adjoint_result* res) {
+    const int T = sp->n_steps;
+    if (T < 1) return fail(s, TDS_ERR_ARG, "adjoint: n_steps must be >= 1");
+    if (!(sp->w_pos >= 0 && sp->w_phi >= 0)) return fail(s, TDS_ERR_ARG, "adjoint: weights must be >= 0");
+    int rc;
+    if ((rc = sync_all(s))) return rc;
+    const size_t N = (size_t)s->N, M = (size_t)s->M, R = (size_t)s->R;
+    const size_t b_state = N * (2 * sizeof(R4<real>) + sizeof(R2<real>) + 2 * sizeof(int));
+    const size_t b_store = b_state + (M + 1) * sizeof(int);
+    const size_t b_snap = b_state + M * sizeof(int) + 2 * (size_t)s->n_tiles * sizeof(int) + 64;
+    const size_t b_fixed = 2 * 3 * N * sizeof(real) + 3 * N * sizeof(R4<real>) + N * tdsk::kGPar * sizeof(double) +
+                           (size_t)T * R * 7 * sizeof(double) + 3 * N * sizeof(double) + b_snap;
+    // checkpoint stride: the largest that fits (one stored segment + the checkpoints)
+    int K = sp->checkpoint_stride;
+    if (K <= 0) {
+        size_t fr = 0, tot = 0;
+        CK(cudaMemGetInfo(&fr, &tot));
+        const double budget = fr > b_fixed ? 0.8 * (double)(fr - b_fixed) : 0.0;
+        for (int k = T; k >= 1; --k) {
+            const double need = (double)((T + k - 1) / k) * (double)b_snap + (double)k * (double)b_store;
+            if (need <= budget) {
+                K = k;
+                break;
+            }
+        }
+        if (K <= 0) return fail(s, TDS_ERR_NOMEM, "adjoint: not enough device memory for one stored step");
+    }
+    K = std::min(K, T);
+    const int nseg = (T + K - 1) / K;
+    const int last0 = (nseg - 1) * K;
+
+    Arena A;
+    std::vector<Snapshot<real>> snaps(nseg);
+    Snapshot<real> fin;
+    for (auto& x : snaps)
+        if (!x.alloc(A, N, M, s->n_tiles)) return fail(s, TDS_ERR_NOMEM, "adjoint: checkpoint allocation");
+    if (!fin.alloc(A, N, M, s->n_tiles)) return fail(s, TDS_ERR_NOMEM, "adjoint: checkpoint allocation");
+    std::vector<StepStore> store(K);
+    for (auto& x : store) {
+        x.pos = A.get<R4<real>>(N), x.pol = A.get<R4<real>>(N), x.uv = A.get<R2<real>>(N);
+        x.ids = A.get<int>(N), x.key = A.get<int>(N), x.start = A.get<int>(M + 1);
+        if (!(x.pos && x.pol && x.uv && x.ids && x.key && x.start))
+            return fail(s, TDS_ERR_NOMEM, "adjoint: segment store allocation");
+        const int nN = s->N;  // the scan writes start[0..M); start[M] = N stays
+        CK(cudaMemcpy(x.start + M, &nN, sizeof(int), cudaMemcpyHostToDevice));
+    }
+    real* lam[2] = {A.get<real>(3 * N), A.get<real>(3 * N)};
+    R4<real>* aF = A.get<R4<real>>(N);
+    R4<real>* aM = A.get<R4<real>>(N);
+    R4<real>* aP = A.get<R4<real>>(N);
+    double* gpar = A.get<double>(N * tdsk::kGPar);
+    double* phisum = A.get<double>((size_t)T * R * 6);
+    double* phibar = A.get<double>((size_t)T * R);
+    double* rtgt = sp->r3d_target ? A.get<double>(3 * N) : nullptr;
+    int* d_off = A.get<int>(R);
+    int* d_cnt = A.get<int>(R);
+    double* d_gp = A.get<double>(R * tdsk::kGPar);
+    if (!(lam[0] && lam[1] && aF && aM && aP && gpar && phisum && phibar && d_off && d_cnt && d_gp) ||
+        (sp->r3d_target && !rtgt))
+        return fail(s, TDS_ERR_NOMEM, "adjoint: work buffer allocation");
+    if ((rc = ensure_series(s, s->step + T))) return rc;
+    free_graphs(s);
+
+    // ---- forward: checkpoints every K steps, the last segment stored step by step ----
+    const long long t_base = s->step;
+    StepHooks hk;
+    hk.phisum = phisum, hk.phisum_base = t_base, hk.phisum_cap = T;
+    for (int t = 0; t < T; ++t) {
+        if (t % K == 0) snapshot_copy<real>(s, snaps[t / K], true);
+        hk.store = t >= last0 ? &store[t - last0] : nullptr;
+        launch_one_step<real>(s, nullptr, &hk);
+    }
+    CK(cudaGetLastError());
+    s->step += T;
+    snapshot_copy<real>(s, fin, true);
+    if ((rc = sync_all(s))) return rc;
+
+    // ---- loss (host, double) ----
+    double loss = 0;
+    std::vector<double> phib((size_t)T * R, 0.0);
+    if (sp->r3d_target && sp->w_pos > 0) {
+        std::vector<double> r3(3 * N);
+        tds_state_view v = {nullptr, nullptr, nullptr, r3.data(), nullptr, nullptr};
+        if ((rc = save_state<real>(s, &v, true))) return rc;
+        for (size_t r = 0; r < R; ++r) {
+            double acc = 0;
+            for (int i = s->off[r]; i < s->off[r] + s->n_rep[r]; ++i)
+                for (int k = 0; k < 3; ++k) {
+                    const double d = r3[3 * (size_t)i + k] - sp->r3d_target[3 * (size_t)i + k];
+                    acc += d * d;
+                }
+            loss += sp->w_pos * acc / s->n_rep[r];
+        }
+        CK(cudaMemcpyAsync(rtgt, sp->r3d_target, 3 * N * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    }
+    const bool phi_term = sp->phi_target && sp->w_phi > 0;
+    if (phi_term) {
+        std::vector<double> ser((size_t)T * 2 * R);
+        CK(cudaMemcpy(ser.data(), s->series + (size_t)t_base * 2 * R, ser.size() * sizeof(double),
+                      cudaMemcpyDeviceToHost));
+        for (int t = 0; t < T; ++t)
+            for (size_t r = 0; r < R; ++r) {
+                const double d = ser[(size_t)t * 2 * R + r] - sp->phi_target[(size_t)t * R + r];
+                loss += sp->w_phi * d * d;
+                phib[(size_t)t * R + r] = 2 * sp->w_phi * d;
+            }
+        CK(cudaMemcpyAsync(phibar, phib.data(), phib.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    }
+    {
+        std::vector<int> off(s->off.begin(), s->off.end()), cnt(s->n_rep.begin(), s->n_rep.end());
+        CK(cudaMemcpyAsync(d_off, off.data(), R * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(d_cnt, cnt.data(), R * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+
+    // ---- reverse sweep ----
+    CK(cudaMemsetAsync(lam[0], 0, 3 * N * sizeof(real), s->stream));
+    CK(cudaMemsetAsync(gpar, 0, N * tdsk::kGPar * sizeof(double), s->stream));
+    int cur = 0;
+    tdsk::AdjArgs<real> a;
+    std::memset(&a, 0, sizeof a);
+    a.desc = s->desc;
+    a.rec = (const real*)s->rec;
+    a.adj = s->adj;
+    a.G = s->G;
+    a.bin_start = s->bin_start;
+    a.bin_faces = s->bin_faces;
+    a.reps = (const RepParams<real>*)s->reps;
+    a.local_bits = s->local_bits;
+    a.cx = (real)s->mesh->t.centroid[0], a.cy = (real)s->mesh->t.centroid[1], a.cz = (real)s->mesh->t.centroid[2];
+    a.seed = s->seed;
+    a.w_pos = sp->w_pos;
+    a.aF = aF, a.aM = aM, a.aP = aP;
+    a.gpar = gpar;
+    a.N = s->N;
+    const int nb = (s->N + 255) / 256;
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+        const int t0 = seg * K, t1 = std::min(T, t0 + K);
+        if (seg != nseg - 1) {  // recompute the segment from its checkpoint, storing each step
+            snapshot_copy<real>(s, snaps[seg], false);
+            StepHooks rk;
+            for (int t = t0; t < t1; ++t) {
+                rk.store = &store[t - t0];
+                launch_one_step<real>(s, nullptr, &rk);
+            }
+        }
+        for (int t = t1 - 1; t >= t0; --t) {
+            const StepStore& x = store[t - t0];
+            a.pos = (const R4<real>*)x.pos, a.pol = (const R4<real>*)x.pol, a.uv = (const R2<real>*)x.uv;
+            a.ids = x.ids, a.key = x.key, a.start = x.start;
+            a.step = t_base + t;
+            a.phisum = phi_term ? phisum + (size_t)t * R * 6 : nullptr;
+            a.phibar = phi_term ? phibar + (size_t)t * R : nullptr;
+            a.r_target = (t == T - 1 && rtgt && sp->w_pos > 0) ? rtgt : nullptr;
+            a.lam_in = lam[cur];
+            a.lam_out = lam[cur ^ 1];
+            tdsk::k_adj_a<real><<<nb, 256, 0, s->stream>>>(a);
+            tdsk::k_adj_b<real><<<nb, 256, 0, s->stream>>>(a);
+            cur ^= 1;
+        }
+    }
+    tdsk::k_adj_reduce<<<(int)R, 256, 0, s->stream>>>(gpar, d_off, d_cnt, d_gp);
+    CK(cudaGetLastError());
+    snapshot_copy<real>(s, fin, false);  // the handle ends where the forward ended
+    std::vector<real> lh(3 * N);
+    std::vector<double> gh(R * tdsk::kGPar);
+    CK(cudaMemcpyAsync(lh.data(), lam[cur], 3 * N * sizeof(real), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(gh.data(), d_gp, gh.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    if ((rc = sync_all(s))) return rc;
+    res->loss = loss;
+    res->checkpoint_stride = K;
+    if (res->d_params)
+        for (size_t i = 0; i < gh.size(); ++i) res->d_params[i] = gh[i];
+    for (size_t i = 0; i < N; ++i) {
+        if (res->d_uv0) res->d_uv0[2 * i] = (double)lh[3 * i], res->d_uv0[2 * i + 1] = (double)lh[3 * i + 1];
+        if (res->d_theta0) res->d_theta0[i] = (double)lh[3 * i + 2];
+    }
+    return TDS_OK;
+}
+
+int check_params(const tds_params& p, std::string& why);
+
+template <typename real>
+int set_params(tds_sim* s, const tds_params* prm) {
+    std::vector<RepParams<real>> rp(s->R);
+    std::memcpy(rp.data(), s->reps_host.data(), rp.size() * sizeof(RepParams<real>));
+    for (int r = 0; r < s->R; ++r) {
+        std::string why;
+        if (check_params(prm[r], why)) return fail(s, TDS_ERR_ARG, "set_params: " + why);
+        if (prm[r].radius != s->prm[r].radius || prm[r].r_max != s->prm[r].r_max)
+            return fail(s, TDS_ERR_ARG, "set_params: radius and r_max fix the cell lists and cannot change");
+        fill_params(rp[r], prm[r]);
+    }
+    int rc;
+    if ((rc = sync_all(s))) return rc;
+    CK(cudaMemcpy(s->reps, rp.data(), rp.size() * sizeof(RepParams<real>), cudaMemcpyHostToDevice));
+    s->reps_host.assign((const unsigned char*)rp.data(), (const unsigned char*)(rp.data() + rp.size()));
+    for (int r = 0; r < s->R; ++r) s->prm[r] = prm[r];
     return TDS_OK;
 }
 
@@ -896,6 +1189,16 @@ int tds_get_state_async(tds_sim* s, tds_state_view* out) {
 int tds_sync(tds_sim* s) {
     if (!s) return TDS_ERR_ARG;
     return sync_all(s);
+}
+
+int tds_set_params(tds_sim* s, const tds_params* params) {
+    if (!s || !params) return TDS_ERR_ARG;
+    return s->precision == 32 ? set_params<float>(s, params) : set_params<double>(s, params);
+}
+
+int tds_adjoint_run(tds_sim* s, const tds_adjoint_spec* spec, tds_adjoint_result* out) {
+    if (!s || !spec || !out) return TDS_ERR_ARG;
+    return s->precision == 32 ? adjoint_run<float>(s, spec, out) : adjoint_run<double>(s, spec, out);
 }
 
 int tds_get_state_noalloc(tds_sim* s, tds_state_view* out) {

@@ -68,7 +68,7 @@ struct RepParams {
     real twoR, inv_twoR, k, adh_scale;  // adh_scale = k_adh / (r_max - 2R)
     real r_max2, v0, mu, inv_tau;
     real align, eta, dt, inv_h;
-    real ox, oy, oz, pad0;                // cell-grid origin
+    real ox, oy, oz, inv_adh_w;           // cell-grid origin; 1 / (r_max - 2R)
     double phiscale;                      // order-parameter fixed point (warp sums -> int64)
     double inv_n;                         // 1 / particles in this replica
     int force_mode, base, C, gx;          // bucket base, surface cells, grid size
@@ -789,9 +789,12 @@ __global__ void __launch_bounds__(kScanThreads) k_tile_sums(const int* __restric
 
 // Order parameter of the step just taken, per replica (one block per replica); zeroes the
 // accumulators.
+// phisum (nullable): the vector sums (sum normalize((r' - c) x v), sum v/|v|) per step and
+// replica, [step - phisum_base][R][6], for the adjoint.
 template <typename real>
 __global__ void k_finalize(unsigned long long* phi_acc, const RepParams<real>* reps, int R, double* series,
-                           long long series_base, long long cap_steps, const long long* d_step) {
+                           long long series_base, long long cap_steps, const long long* d_step, double* phisum,
+                           long long phisum_base, long long phisum_cap) {
     __shared__ double s[kPhiCopies * 6];
     const int r = blockIdx.x;
     const int t = threadIdx.x;
@@ -814,6 +817,9 @@ __global__ void k_finalize(unsigned long long* phi_acc, const RepParams<real>* r
             series[(size_t)tt * 2 * R + r] = phi;
             series[(size_t)tt * 2 * R + R + r] = psi;
         }
+        const long long tp = *d_step - phisum_base;
+        if (phisum && tp >= 0 && tp < phisum_cap)
+            for (int k = 0; k < 6; ++k) phisum[((size_t)tp * R + r) * 6 + k] = v[k] * inv;
     }
 }
 

@@ -130,6 +130,40 @@ int tds_get_state_async(tds_sim* sim, tds_state_view* out);
 /* Waits for all work of the handle (transfers and steps); TDS_ERR_STATE if the device status
  * word is non-zero. */
 int tds_sync(tds_sim* sim);
+
+/* Replaces the model parameters (params has one entry per replica). radius and r_max fix the
+ * cell lists and must stay as created (TDS_ERR_ARG otherwise); the state is kept. The reference
+ * fixes its parameters in the _2DTissue constructor (2DTissue.h:37-54). */
+int tds_set_params(tds_sim* sim, const tds_params* params);
+
+/* ---- adjoint (no counterpart in the reference; SURVEY-planned entry point tds_adjoint_run) ----
+ * Loss over a run of n_steps from the current state:
+ *   L = w_pos * sum_r (1/N_r) sum_{i in r} |r_T,i - r*_i|^2  +  w_phi * sum_t sum_r (phi_t,r - phi*_t,r)^2
+ * with r_T the 3D positions after the last step and phi_t the order parameter of step t. The
+ * gradients are those of the step with neighbour sets, faces and seam-wrap sequences held at the
+ * forward run's (reverse mode, hand-written), with Philox noise fixed by the seed. The initial
+ * 3D positions are taken as the chart map of the initial uv (r = A_f + J_f (uv - a_f)). */
+typedef struct tds_adjoint_spec {
+    int n_steps;
+    int checkpoint_stride;     /* steps between checkpoints; 0 = the largest that fits in memory */
+    const double* r3d_target;  /* 3N in id order, or NULL (no position term) */
+    double w_pos;
+    const double* phi_target;  /* n_steps x n_replicas, step-major, or NULL (no order-parameter term) */
+    double w_phi;
+} tds_adjoint_spec;
+typedef struct tds_adjoint_result {
+    double loss;
+    /* n_replicas x 8: dL/d(k_rep, k_adh, v0, mu, tau, align, eta), 0 (may be NULL) */
+    double* d_params;
+    double* d_uv0;     /* 2N, dL/d(initial uv) in id order (may be NULL) */
+    double* d_theta0;  /* N, dL/d(initial polarity angle) (may be NULL) */
+    int checkpoint_stride; /* out: the stride used */
+} tds_adjoint_result;
+/* Runs n_steps forward (the handle advances exactly as tds_step would), storing a checkpoint every
+ * checkpoint_stride steps, evaluates L, then the reverse sweep: segment by segment from the last,
+ * recomputing each segment from its checkpoint with every step's sorted state kept, and two
+ * kernels per step. */
+int tds_adjoint_run(tds_sim* sim, const tds_adjoint_spec* spec, tds_adjoint_result* out);
 /* Per-kernel CUDA-event timing of directly launched steps (graphs are not used while enabled).
  * tds_kernel_times returns, per kernel (0 scan, 1 scatter, 2 order, 3 step, 4 finalize), the
  * summed device time in ms and the launch count since timing was enabled (arrays of 5). */
