@@ -452,6 +452,55 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
+def run_adjoint_batched(args):
+    """Batched adjoint for parameter inference: 512 replicas on the bumpy sphere
+    r = 1 + 0.2 Re Y_4^2 scaled x5 (level-6 icosphere), particle counts uniform in [1000, 20000],
+    per-replica v0 U[0.5,1.5], k U[5,20], tau U[0.5,2], eta U[0.1,1]; R 0.05, dt 0.02, FP32,
+    `steps` steps (default 500), checkpoint stride chosen to fit device memory. Target: the same
+    replicas run with v0 1, k 10, tau 1, eta 0.5. Forward arm: tds_step over the same steps."""
+    import torch
+    tg = importlib.import_module("2dtissue_gb300")
+    mesh = tg.Mesh.bumpy_sphere(6, 0.2, 5.0)
+    rng = np.random.default_rng(5)
+    R = 512
+    T = args.steps if args.steps != 50 else 500
+    ns = [int(x) for x in rng.integers(1000, 20001, size=R)]
+    ps = [tg.Params(v0=float(rng.uniform(0.5, 1.5)), k_rep=float(rng.uniform(5, 20)), tau=float(rng.uniform(0.5, 2)),
+                    eta=float(rng.uniform(0.1, 1.0))) for _ in range(R)]
+    ref = tg.Simulation(mesh, [tg.Params(v0=1.0, k_rep=10.0, tau=1.0, eta=0.5)] * R, ns, seed=1, precision=32)
+    ref.start()
+    s0 = ref.get_state()
+    ref.step(T)
+    r_star = ref.get_state()["r3d"]
+    phi_star = ref.order_parameter()[0][-T:].copy()
+    ref.close()
+    sim = tg.Simulation(mesh, ps, ns, seed=1, precision=32)
+    sim.set_state(s0["uv"], s0["theta"], s0["face"])
+    sim.step(16)
+    sim.set_state(s0["uv"], s0["theta"], s0["face"])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.step(T)
+    fwd_s = time.perf_counter() - t0
+    sim.set_state(s0["uv"], s0["theta"], s0["face"])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = sim.adjoint(T, r3d_target=r_star, w_pos=1.0, phi_target=phi_star, w_phi=1.0)
+    adj_s = time.perf_counter() - t0
+    total = int(sum(ns))
+    g = res["d_params"]
+    line = {"metric": "particle-steps/s (forward+adjoint, batched ragged ensemble, 512 replicas)",
+            "value": total * T / adj_s, "unit": UNIT, "n_gpus": 1, "steps": T, "warmup": 1, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": "batched adjoint, bumpy sphere 1+0.2 Re Y_4^2 x5, L6 icosphere, 512 replicas, "
+                                   "N U[1000,20000], per-replica v0/k/tau/eta", "replicas": R, "particles": total,
+                       "steps": T, "checkpoint_stride": res["checkpoint_stride"]},
+            "forward": {"value": total * T / fwd_s, "unit": UNIT, "path": "tds_step (CUDA graphs)"},
+            "adjoint_over_forward": adj_s / fwd_s, "loss": res["loss"],
+            "finite_gradients": bool(np.isfinite(g).all()), "replicas_with_finite_gradients": int(np.isfinite(g).all(1).sum())}
+    print(json.dumps(line), flush=True)
+
+
 def run_profile(args):
     """Minimal driver for ncu: the config-2 system, `warmup` steps, then `steps` steps; no timing."""
     import torch
@@ -474,7 +523,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", action="store_true", help="only run warmup + steps (for ncu)")
-    ap.add_argument("--workload", default="plain", choices=["plain", "ensemble", "adjoint"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "ensemble", "adjoint", "adjoint_batched"])
     ap.add_argument("--replicas", type=int, default=4096, help="ensemble workload: replicas")
     ap.add_argument("--sample", type=int, default=256, help="ensemble workload: replicas run one by one")
     args = ap.parse_args()
@@ -484,6 +533,8 @@ def main():
         return run_ensemble(args)
     if args.workload == "adjoint" and args.impl != "reference":
         return run_adjoint(args)
+    if args.workload == "adjoint_batched" and args.impl != "reference":
+        return run_adjoint_batched(args)
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":
