@@ -223,8 +223,9 @@ __global__ void __launch_bounds__(256) k_adj_a(const AdjArgs<real> a) {
         }
     }
     // r2 = A' + J' (uv3 - a')
-    ub3x += h[8] * rb2[0] + h[9] * rb2[1] + h[10] * rb2[2];
-    ub3y += h[11] * rb2[0] + h[12] * rb2[1] + h[13] * rb2[2];
+    const R4<real> h2 = rq(h, 2), h3 = rq(h, 3);
+    ub3x += h2.x * rb2[0] + h2.y * rb2[1] + h2.z * rb2[2];
+    ub3y += h2.w * rb2[0] + h3.x * rb2[1] + h3.y * rb2[2];
     // uv3 = R uv2 + t
     const real ub2x = R00 * ub3x + R10 * ub3y, ub2y = R01 * ub3x + R11 * ub3y;
     // uv2 = uv + dt (Jp v)
@@ -344,19 +345,21 @@ __global__ void __launch_bounds__(256) k_adj_b(const AdjArgs<real> a) {
         }
     });
     // r = A + J (uv - a)
-    const real ubx = myF.w + g[8] * rb[0] + g[9] * rb[1] + g[10] * rb[2];
-    const real uby = myM.w + g[11] * rb[0] + g[12] * rb[1] + g[13] * rb[2];
+    const R4<real> g2 = rq(g, 2), g3 = rq(g, 3);
+    const real Ju[3] = {g2.x, g2.y, g2.z}, Jv[3] = {g2.w, g3.x, g3.y};
+    const real ubx = myF.w + Ju[0] * rb[0] + Ju[1] * rb[1] + Ju[2] * rb[2];
+    const real uby = myM.w + Jv[0] * rb[0] + Jv[1] * rb[1] + Jv[2] * rb[2];
     // p = normalize(J (cos th, sin th))
     const real pbt[3] = {myP.x + msum[0], myP.y + msum[1], myP.z + msum[2]};
     real sn, cs;
     d_sincos(P.w, &sn, &cs);
-    const real qv[3] = {g[8] * cs + g[11] * sn, g[9] * cs + g[12] * sn, g[10] * cs + g[13] * sn};
+    const real qv[3] = {Ju[0] * cs + Jv[0] * sn, Ju[1] * cs + Jv[1] * sn, Ju[2] * cs + Jv[2] * sn};
     const real iq = d_rsqrt(dot(qv, qv));
     const real pp[3] = {qv[0] * iq, qv[1] * iq, qv[2] * iq};
     const real pq = dot(pbt, pp);
     const real qb[3] = {(pbt[0] - pq * pp[0]) * iq, (pbt[1] - pq * pp[1]) * iq, (pbt[2] - pq * pp[2]) * iq};
-    const real cb0 = g[8] * qb[0] + g[9] * qb[1] + g[10] * qb[2];
-    const real cb1 = g[11] * qb[0] + g[12] * qb[1] + g[13] * qb[2];
+    const real cb0 = Ju[0] * qb[0] + Ju[1] * qb[1] + Ju[2] * qb[2];
+    const real cb1 = Jv[0] * qb[0] + Jv[1] * qb[1] + Jv[2] * qb[2];
     a.lam_out[3 * (size_t)gid] = ubx;
     a.lam_out[3 * (size_t)gid + 1] = uby;
     a.lam_out[3 * (size_t)gid + 2] = -sn * cb0 + cs * cb1;

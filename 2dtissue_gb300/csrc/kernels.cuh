@@ -144,12 +144,20 @@ __device__ __forceinline__ real kPi() {
     return (real)3.14159265358979323846;
 }
 
+// Quad k (reals 4k..4k+3) of a face record: records are 16 reals aligned to their size, so each
+// is read with four vector loads instead of sixteen scalar ones.
+template <typename real>
+__device__ __forceinline__ R4<real> rq(const real* r, int k) {
+    return reinterpret_cast<const R4<real>*>(r)[k];
+}
+
 // unit 3D polarity from the chart angle on face record g: normalize(J (cos th, sin th))
 template <typename real>
 __device__ __forceinline__ void polarity3(const real* g, real th, real& px, real& py, real& pz) {
     real sn, cs;
     d_sincos(th, &sn, &cs);
-    const real qx = g[8] * cs + g[11] * sn, qy = g[9] * cs + g[12] * sn, qz = g[10] * cs + g[13] * sn;
+    const R4<real> q2 = rq(g, 2), q3 = rq(g, 3);
+    const real qx = q2.x * cs + q2.w * sn, qy = q2.y * cs + q3.x * sn, qz = q2.z * cs + q3.y * sn;
     const real qn = d_sqrt(qx * qx + qy * qy + qz * qz);
     px = qx / qn, py = qy / qn, pz = qz / qn;
 }
@@ -163,8 +171,9 @@ __device__ __forceinline__ real orient(real Px, real Py, real Qx, real Qy, real 
 }
 template <typename real>
 __device__ __forceinline__ void edge_values(const real* r, real px, real py, real e[3]) {
-    const int bits = (int)r[6];
-    const real P[3][2] = {{r[0], r[1]}, {r[2], r[3]}, {r[4], r[5]}};
+    const R4<real> q0 = rq(r, 0), q1 = rq(r, 1);
+    const int bits = (int)q1.z;
+    const real P[3][2] = {{q0.x, q0.y}, {q0.z, q0.w}, {q1.x, q1.y}};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const int k1 = (k + 1) % 3;
@@ -182,11 +191,13 @@ template <typename real>
 __device__ __forceinline__ real face_score(const real* r, real px, real py) {
     real e[3];
     edge_values(r, px, py, e);
+    const R4<real> q0 = rq(r, 0), q1 = rq(r, 1);
+    const real c[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
     real s = (real)1e30;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const int k1 = (k + 1) % 3;
-        const real ex = r[2 * k1] - r[2 * k], ey = r[2 * k1 + 1] - r[2 * k + 1];
+        const real ex = c[2 * k1] - c[2 * k], ey = c[2 * k1 + 1] - c[2 * k + 1];
         s = fmin(s, e[k] / d_sqrt(ex * ex + ey * ey));
     }
     return s;
@@ -195,7 +206,8 @@ __device__ __forceinline__ real face_score(const real* r, real px, real py) {
 // Unit normal and pseudo-inverse Jp = (J^T J)^-1 J^T of a face's chart map.
 template <typename real>
 __device__ __forceinline__ void face_frame(const real* g, real n[3], real Jp[6]) {
-    const real ux = g[8], uy = g[9], uz = g[10], vx = g[11], vy = g[12], vz = g[13];
+    const R4<real> q2 = rq(g, 2), q3 = rq(g, 3);
+    const real ux = q2.x, uy = q2.y, uz = q2.z, vx = q2.w, vy = q3.x, vz = q3.y;
     const real cx = uy * vz - uz * vy, cy = uz * vx - ux * vz, cz = ux * vy - uy * vx;
     const real ic = d_rsqrt(cx * cx + cy * cy + cz * cz);
     n[0] = cx * ic, n[1] = cy * ic, n[2] = cz * ic;
@@ -209,10 +221,11 @@ __device__ __forceinline__ void face_frame(const real* g, real n[3], real Jp[6])
 // chart point -> 3D on face record h
 template <typename real>
 __device__ __forceinline__ void face_map(const real* h, real u, real v, real& x, real& y, real& z) {
-    const real du = u - h[0], dv = v - h[1];
-    x = h[7] + h[8] * du + h[11] * dv;
-    y = h[14] + h[9] * du + h[12] * dv;
-    z = h[15] + h[10] * du + h[13] * dv;
+    const R4<real> q0 = rq(h, 0), q1 = rq(h, 1), q2 = rq(h, 2), q3 = rq(h, 3);
+    const real du = u - q0.x, dv = v - q0.y;
+    x = q1.w + q2.x * du + q2.w * dv;
+    y = q3.z + q2.y * du + q3.x * dv;
+    z = q3.w + q2.z * du + q3.y * dv;
 }
 template <typename real>
 __device__ __forceinline__ int bin_coord(real x, int G) {
@@ -541,7 +554,8 @@ __global__ void __launch_bounds__(kStepThreads, sizeof(real) == 4 ? 5 : 3) k_ste
         // new 3D polarity: normalize(J_f2 w) (= normalize(J_f2 (cos th, sin th)))
         real qx, qy, qz;
         {
-            const real ex = h[8] * w0 + h[11] * w1, ey = h[9] * w0 + h[12] * w1, ez = h[10] * w0 + h[13] * w1;
+            const R4<real> h2 = rq(h, 2), h3 = rq(h, 3);
+            const real ex = h2.x * w0 + h2.w * w1, ey = h2.y * w0 + h3.x * w1, ez = h2.z * w0 + h3.y * w1;
             const real ien = d_rsqrt(ex * ex + ey * ey + ez * ez);
             qx = ex * ien, qy = ey * ien, qz = ez * ien;
         }
