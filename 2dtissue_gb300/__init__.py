@@ -120,7 +120,7 @@ def _ptr(a):
 
 @dataclass
 class Params:
-    """Model parameters; defaults are the config-1 values (radius 0.05, r_max = 2.4 R)."""
+    """Model parameters; defaults are those of the 100-particle (2,1,1)-ellipsoid system (radius 0.05, r_max = 2.4 R)."""
     radius: float = 0.05
     k_rep: float = 10.0
     k_adh: float = 0.75

@@ -91,6 +91,7 @@ struct tds_sim {
     int* start = nullptr;
     int* count = nullptr;
     unsigned long long* phi_acc = nullptr;
+    int* phi_pending = nullptr;  // a step's order parameter awaits finalizing (next k_scan or a flush)
     double* series = nullptr;
     long long series_cap = 0;  // steps
     int* status = nullptr;
@@ -309,6 +310,7 @@ int alloc_state(tds_sim* s) {
     if ((rc = dalloc(s, &s->tile_sum, (size_t)2 * s->n_tiles * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->phi_acc, (size_t)s->R * tdsk::kPhiCopies * 6 * sizeof(unsigned long long)))) return rc;
     if ((rc = dalloc(s, &s->status, sizeof(int)))) return rc;
+    if ((rc = dalloc(s, &s->phi_pending, sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->d_step, sizeof(long long)))) return rc;
     if ((rc = dalloc(s, &s->packed_ids, N * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->st_d, 8 * N * sizeof(double)))) return rc;
@@ -319,6 +321,7 @@ int alloc_state(tds_sim* s) {
     CK(cudaMemset(s->tile_sum, 0, (size_t)2 * s->n_tiles * sizeof(int)));
     CK(cudaMemset(s->phi_acc, 0, (size_t)s->R * tdsk::kPhiCopies * 6 * sizeof(unsigned long long)));
     CK(cudaMemset(s->status, 0, sizeof(int)));
+    CK(cudaMemset(s->phi_pending, 0, sizeof(int)));
     const int nN = s->N;
     CK(cudaMemcpy(s->start + s->M, &nN, sizeof(int), cudaMemcpyHostToDevice));
     const long long m1 = -1;
@@ -411,6 +414,32 @@ struct StepHooks {
     long long phisum_base = 0, phisum_cap = 0;
 };
 
+template <typename real>
+tdsk::FinArgs<real> fin_args(tds_sim* s, const StepHooks* hk) {
+    tdsk::FinArgs<real> f;
+    f.phi_acc = s->phi_acc;
+    f.reps = (const RepParams<real>*)s->reps;
+    f.R = s->R;
+    f.series = s->series;
+    f.cap_steps = s->series_cap;
+    f.phisum = hk ? hk->phisum : nullptr;
+    f.phisum_base = hk ? hk->phisum_base : 0;
+    f.phisum_cap = hk ? hk->phisum_cap : 0;
+    f.pending = s->phi_pending;
+    return f;
+}
+
+// Finalizes the order parameter of the last step if no k_scan has done it yet (before the series
+// is read).
+template <typename real>
+void flush_finalize(tds_sim* s, const StepHooks* hk = nullptr) {
+    {
+        KernelTimer kt(s, 4);
+        tdsk::k_finalize<real><<<s->R, 128, 0, s->stream>>>(fin_args<real>(s, hk), s->d_step);
+    }
+    cudaMemsetAsync(s->phi_pending, 0, sizeof(int), s->stream);
+}
+
 // Buffer roles: index 0 = step output (and set_state target), index 1 = sorted copy.
 template <typename real>
 void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullptr) {
@@ -427,13 +456,13 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
     int* start = x ? x->start : s->start;
     {
         KernelTimer kt(s, 0);
-        tdsk::k_scan<<<s->n_tiles, tdsk::kScanThreads, 0, st>>>(s->count, start, s->M, s->tile_sum, s->n_tiles,
-                                                                 s->d_step);
+        tdsk::k_scan<real><<<s->n_tiles + s->R, tdsk::kScanThreads, 0, st>>>(
+            s->count, start, s->M, s->tile_sum, s->n_tiles, s->d_step, fin_args<real>(s, hk));
     }
     const int nb = (s->N + 255) / 256;
     {
         KernelTimer kt(s, 1);
-        tdsk::k_scatter<<<nb, 256, 0, st>>>(s->key[o], s->count, start, s->tmp, s->N, s->d_step);
+        tdsk::k_scatter<<<nb, 256, 0, st>>>(s->key[o], s->count, start, s->tmp, s->N, s->d_step, s->phi_pending);
     }
     {
         KernelTimer kt(s, 2);
@@ -471,6 +500,7 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
     a.cx = (real)s->mesh->t.centroid[0], a.cy = (real)s->mesh->t.centroid[1], a.cz = (real)s->mesh->t.centroid[2];
     a.noise = noise;
     a.phi_acc = s->phi_acc;
+    a.phi_pending = s->phi_pending;
     a.d_step = s->d_step;
     a.seed = s->seed;
     a.status = s->status;
@@ -479,12 +509,6 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
     {
         KernelTimer kt(s, 3);
         tdsk::k_step<real><<<ns, tdsk::kStepThreads, 0, st>>>(a);
-    }
-    {
-        KernelTimer kt(s, 4);
-        tdsk::k_finalize<real><<<s->R, 128, 0, st>>>(
-            s->phi_acc, (const RepParams<real>*)s->reps, s->R, s->series, 0, s->series_cap, s->d_step,
-            hk ? hk->phisum : nullptr, hk ? hk->phisum_base : 0, hk ? hk->phisum_cap : 0);
     }
 }
 
@@ -758,6 +782,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp, tds_adjoint_result* res)
         hk.store = t >= last0 ? &store[t - last0] : nullptr;
         launch_one_step<real>(s, nullptr, &hk);
     }
+    flush_finalize<real>(s, &hk);
     CK(cudaGetLastError());
     s->step += T;
     snapshot_copy<real>(s, fin, true);
@@ -831,6 +856,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp, tds_adjoint_result* res)
                 rk.store = &store[t - t0];
                 launch_one_step<real>(s, nullptr, &rk);
             }
+            flush_finalize<real>(s);  // the next restore must not finalize this segment's last step
         }
         for (int t = t1 - 1; t >= t0; --t) {
             const StepStore& x = store[t - t0];
@@ -1211,6 +1237,10 @@ int tds_get_order_parameter(tds_sim* s, double* phi, double* psi, int cap, int* 
     const long long n = std::min<long long>(s->step, s->series_cap);
     if (n_steps) *n_steps = (int)n;
     if (n == 0 || cap <= 0) return TDS_OK;
+    if (s->precision == 32)
+        flush_finalize<float>(s);
+    else
+        flush_finalize<double>(s);
     std::vector<double> tmp((size_t)n * 2 * s->R);
     CK(cudaMemcpyAsync(tmp.data(), s->series, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
@@ -1258,7 +1288,7 @@ int tds_stream(tds_sim* s, void** stream) {
 
 int tds_kernels_per_step(const tds_sim* s, int* n) {
     if (!s || !n) return TDS_ERR_ARG;
-    *n = 5;
+    *n = 4;
     return TDS_OK;
 }
 

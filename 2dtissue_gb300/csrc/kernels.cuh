@@ -1,8 +1,9 @@
 // sm_103a kernels of the per-step particle update.
 //
-// One step is five launches on the handle's stream (captured in a CUDA graph by the host):
+// One step is four launches on the handle's stream (captured in a CUDA graph by the host):
 //   k_scan     exclusive scan of the cell-list counts; block bases from per-tile counts that the
-//              previous step accumulated (no inter-block waiting)
+//              previous step accumulated (no inter-block waiting); R extra blocks finalize the
+//              previous step's order parameter per replica
 //   k_scatter  counting-sort scatter: tmp[start[key] + rank] = slot (rank from atomics)
 //   k_order    orders each cell's particles by particle id (so that the neighbour visiting order,
 //              and every floating-point sum, is the same on every run) and writes the state in
@@ -10,7 +11,7 @@
 //              candidates of a cell run from consecutive addresses
 //   k_step     fused pair sums + tangent projection + polarity update + chart advance + seam
 //              wrap + face location + chart->3D map + next-step cell key/count + order partials
-//   k_finalize order parameter per replica for this step
+// (k_finalize runs the same per-replica finalize on its own before the series is read.)
 // Replaces (reference): Locomotion::simulate_flight + ForceHelper + OrientationHelper
 // (Locomotion.cpp:57-162, ForceHelper.cpp:34-104, OrientationHelper.cpp:29-116),
 // EuclideanTiling::diagonal_seam_edges_square_border (EuclideanTiling.cpp:31-208),
@@ -108,6 +109,7 @@ struct StepArgs {
     real cx, cy, cz;
     const real* noise;  // nullable: angle increments by global particle index
     unsigned long long* phi_acc;
+    int* phi_pending;  // set: this step's order parameter awaits finalizing
     const long long* d_step;
     unsigned long long seed;
     int* status;
@@ -447,8 +449,9 @@ __global__ void __launch_bounds__(kStepThreads, sizeof(real) == 4 ? 5 : 3) k_ste
         const real* g = a.rec + (size_t)f * kRec;
         const real px = PL.x, py = PL.y, pz = PL.z;
 
-        // candidate ranges: the 9 x-runs of the particle's cell (static descriptors)
-        int rs[9], rc[9];
+        // candidate ranges: the 9 x-runs of the particle's cell (static descriptors), as
+        // (first slot, count) pairs so that the loop switches runs with one 8-byte load
+        int2 run[9];
         int total = 0;
         const int id0 = key0 - rp.base;
         if (id0 < rp.C) {
@@ -461,32 +464,31 @@ __global__ void __launch_bounds__(kStepThreads, sizeof(real) == 4 ? 5 : 3) k_ste
                 const int b0 = rp.base + first;
                 const int t0 = len ? a.start[b0] : 0;
                 const int t1 = len ? a.start[b0 + len] : 0;
-                rs[r] = t0;
-                rc[r] = t1 - t0;
+                run[r] = make_int2(t0, t1 - t0);
                 total += t1 - t0;
             }
         } else {
 #pragma unroll
-            for (int r = 0; r < 9; ++r) rs[r] = 0, rc[r] = 0;
+            for (int r = 0; r < 9; ++r) run[r] = make_int2(0, 0);
         }
         // pair sums over all candidates (in a fixed order), two per iteration
         real acc[6] = {0, 0, 0, 0, 0, 0};
         int cnt = 0;
-        int r = 0, t = rs[0], left = rc[0];
+        int r = 0, t = run[0].x, left = run[0].y;
         for (int k = 0; k < total; k += 2) {
             while (left == 0) {
-                ++r;
-                t = rs[r];
-                left = rc[r];
+                const int2 x = run[++r];
+                t = x.x;
+                left = x.y;
             }
             const int ta = t++;
             --left;
             int tb = -1;
             if (k + 1 < total) {
                 while (left == 0) {
-                    ++r;
-                    t = rs[r];
-                    left = rc[r];
+                    const int2 x = run[++r];
+                    t = x.x;
+                    left = x.y;
                 }
                 tb = t++;
                 --left;
@@ -618,6 +620,7 @@ __global__ void __launch_bounds__(kStepThreads, sizeof(real) == 4 ? 5 : 3) k_ste
         }
     }
     if (st) atomicOr(a.status, st);
+    if (q == 0) *a.phi_pending = 1;
 
     // order-parameter reduction: warp sum (same replica) -> atomics on one of kPhiCopies slots
     const unsigned FULL = 0xffffffffu;
@@ -652,16 +655,69 @@ __global__ void __launch_bounds__(kStepThreads, sizeof(real) == 4 ? 5 : 3) k_ste
 }
 
 // ---------------------------------------------------------------------------------------------
+// order parameter of a step, per replica
+// ---------------------------------------------------------------------------------------------
+template <typename real>
+struct FinArgs {
+    unsigned long long* phi_acc;  // [R][kPhiCopies][6] fixed-point sums of the step just taken
+    const RepParams<real>* reps;
+    int R;
+    double* series;  // [cap_steps][2][R]: phi, psi by step
+    long long cap_steps;
+    double* phisum;  // nullable: the vector sums (sum normalize((r' - c) x v), sum v/|v|),
+                     // [step - phisum_base][R][6], for the adjoint
+    long long phisum_base, phisum_cap;
+    int* pending;  // set by k_step, cleared by k_scatter and after a standalone finalize
+};
+
+// One block: replica r's order parameter of `step` into the series; zeroes its accumulators.
+template <typename real>
+__device__ void finalize_replica(const FinArgs<real>& f, int r, long long step, double* s) {
+    const int t = threadIdx.x;
+    for (int i = t; i < kPhiCopies * 6; i += blockDim.x) {
+        unsigned long long* p = &f.phi_acc[(size_t)r * kPhiCopies * 6 + i];
+        s[i] = (double)(long long)(*p);
+        *p = 0ull;
+    }
+    __syncthreads();
+    if (t == 0) {
+        double v[6] = {0, 0, 0, 0, 0, 0};
+        for (int c = 0; c < kPhiCopies; ++c)
+            for (int k = 0; k < 6; ++k) v[k] += s[c * 6 + k];
+        const RepParams<real>& rp = f.reps[r];
+        const double inv = 1.0 / rp.phiscale;
+        const double phi = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) * inv * rp.inv_n;
+        const double psi = sqrt(v[3] * v[3] + v[4] * v[4] + v[5] * v[5]) * inv * rp.inv_n;
+        if (step >= 0 && step < f.cap_steps) {
+            f.series[(size_t)step * 2 * f.R + r] = phi;
+            f.series[(size_t)step * 2 * f.R + f.R + r] = psi;
+        }
+        const long long tp = step - f.phisum_base;
+        if (f.phisum && tp >= 0 && tp < f.phisum_cap)
+            for (int k = 0; k < 6; ++k) f.phisum[((size_t)tp * f.R + r) * 6 + k] = v[k] * inv;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
 // cell-list kernels
 // ---------------------------------------------------------------------------------------------
 // Exclusive scan of count[0..M) into start[0..M). Each block's base is the sum of
 // the per-tile counts of the tiles before it (accumulated by the previous step), so no block
 // waits on another. Also zeroes the other parity's tile counts for the step about to run.
+// The R blocks past the n_tiles scan blocks finalize the previous step's order parameter (when a
+// step is pending), so that it costs no launch of its own.
+template <typename real>
 __global__ void __launch_bounds__(kScanThreads) k_scan(int* __restrict__ count, int* __restrict__ start, long long M,
                                                        int* __restrict__ tile_sum, int n_tiles,
-                                                       const long long* d_step) {
+                                                       const long long* d_step, const FinArgs<real> fin) {
     __shared__ int s_warp[kScanThreads / 32];
     __shared__ int s_base;
+    if ((int)blockIdx.x >= n_tiles) {
+        __shared__ double s_fin[kPhiCopies * 6];
+        if (*fin.pending == 0) return;
+        finalize_replica(fin, (int)blockIdx.x - n_tiles, *d_step, s_fin);
+        return;
+    }
     const int par = (int)((*d_step + 1) & 1);
     const int* ts = tile_sum + (size_t)par * n_tiles;
     const int tile = blockIdx.x;
@@ -740,9 +796,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(int* __restrict__ count, 
 
 // Counting-sort scatter; the cell's count is the cursor and ends at zero for the next step.
 __global__ void k_scatter(const int* __restrict__ key, int* __restrict__ count, const int* __restrict__ start,
-                          int* __restrict__ tmp, int N, long long* d_step) {
+                          int* __restrict__ tmp, int N, long long* d_step, int* phi_pending) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s == 0) *d_step += 1;
+    if (s == 0) {
+        *d_step += 1;
+        *phi_pending = 0;  // k_scan has finalized the previous step
+    }
     if (s < N) {
         const int b = key[s];
         tmp[start[b] + atomicSub(&count[b], 1) - 1] = s;
@@ -803,38 +862,13 @@ __global__ void __launch_bounds__(kScanThreads) k_tile_sums(const int* __restric
 
 // Order parameter of the step just taken, per replica (one block per replica); zeroes the
 // accumulators.
-// phisum (nullable): the vector sums (sum normalize((r' - c) x v), sum v/|v|) per step and
-// replica, [step - phisum_base][R][6], for the adjoint.
+// Standalone finalize (the flush before the series is read): the same as the blocks that k_scan
+// runs past its tiles, for a step that no k_scan has followed yet.
 template <typename real>
-__global__ void k_finalize(unsigned long long* phi_acc, const RepParams<real>* reps, int R, double* series,
-                           long long series_base, long long cap_steps, const long long* d_step, double* phisum,
-                           long long phisum_base, long long phisum_cap) {
+__global__ void k_finalize(const FinArgs<real> f, const long long* d_step) {
     __shared__ double s[kPhiCopies * 6];
-    const int r = blockIdx.x;
-    const int t = threadIdx.x;
-    for (int i = t; i < kPhiCopies * 6; i += blockDim.x) {
-        unsigned long long* p = &phi_acc[(size_t)r * kPhiCopies * 6 + i];
-        s[i] = (double)(long long)(*p);
-        *p = 0ull;
-    }
-    __syncthreads();
-    if (t == 0) {
-        double v[6] = {0, 0, 0, 0, 0, 0};
-        for (int c = 0; c < kPhiCopies; ++c)
-            for (int k = 0; k < 6; ++k) v[k] += s[c * 6 + k];
-        const RepParams<real>& rp = reps[r];
-        const double inv = 1.0 / rp.phiscale;
-        const double phi = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) * inv * rp.inv_n;
-        const double psi = sqrt(v[3] * v[3] + v[4] * v[4] + v[5] * v[5]) * inv * rp.inv_n;
-        const long long tt = *d_step - series_base;
-        if (tt >= 0 && tt < cap_steps) {
-            series[(size_t)tt * 2 * R + r] = phi;
-            series[(size_t)tt * 2 * R + R + r] = psi;
-        }
-        const long long tp = *d_step - phisum_base;
-        if (phisum && tp >= 0 && tp < phisum_cap)
-            for (int k = 0; k < 6; ++k) phisum[((size_t)tp * R + r) * 6 + k] = v[k] * inv;
-    }
+    if (*f.pending == 0) return;
+    finalize_replica(f, (int)blockIdx.x, *d_step, s);
 }
 
 // State (physical order) -> id order, in double.

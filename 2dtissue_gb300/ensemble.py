@@ -6,7 +6,7 @@ exchange; only the per-replica order-parameter series are gathered at the end.
 import numpy as np
 
 
-def config3_replicas(seed=0, n_replicas=4096):
+def ragged_replicas(seed=0, n_replicas=4096):
     """The batched ragged ensemble: particle counts log-uniform in [64, 8192], eta uniform in
     [0, 2 pi], v0 uniform in [0.5, 1.5] (seeded)."""
     rng = np.random.default_rng(seed)

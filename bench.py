@@ -5,7 +5,7 @@ Workload (the headline configuration): the (20,10,10) ellipsoid meshed as a leve
 (163,842 vertices, 327,680 faces), 1,048,576 particles at area packing 0.5 (radius from packing,
 r_max = 2.4 R), eta = 0.3, dt = 0.01, FP32 state. Synthetic, seeded placement (no dataset exists).
 
-One bench step = one simulation step of the whole system (5 kernels). L2 is flushed (a 256 MB
+One bench step = one simulation step of the whole system (4 kernels). L2 is flushed (a 256 MB
 write, outside the timed window) before every timed step; each step is timed with CUDA events on
 the handle's stream. value = particle-steps/s over all ranks (max time over ranks).
 e2e = the same metric through the C-ABI with host buffers: set_state (H2D) + step + get_state (D2H)
@@ -36,7 +36,7 @@ ALG_BYTES_FACE = 60      # 3 UV corners x 8 + 3 3D corners x 12
 ALG_BYTES_REPLICA = 4    # order parameter
 
 
-def config2(tg):
+def workload_1m(tg):
     mesh = tg.Mesh.ellipsoid(7, (20.0, 10.0, 10.0))
     n = 1 << 20
     radius = float(np.sqrt(0.5 * mesh.area / (np.pi * n)))
@@ -60,7 +60,7 @@ def measured_peak():
 
 def profiled_traffic(n_particles):
     """DRAM bytes per k_step launch from the committed ncu summary (scaled to n_particles)."""
-    path = os.path.join(ROOT, "profiles", "k_step_config2.md")
+    path = os.path.join(ROOT, "profiles", "k_step_1m_particles.md")
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_particle:"):
@@ -176,7 +176,7 @@ def run_reference(args):
     if rank != 0:
         return
     tg = importlib.import_module("2dtissue_gb300")
-    mesh, p, n = config2(tg)
+    mesh, p, n = workload_1m(tg)
     state = seeded_state(mesh, n, 0)
     import oracle
     a = mesh.arrays()
@@ -217,7 +217,7 @@ def run_gpu(args):
         raise SystemExit("bench.py needs a CUDA GPU")
     torch.cuda.set_device(local)
     tg = importlib.import_module("2dtissue_gb300")
-    mesh, p, n = config2(tg)
+    mesh, p, n = workload_1m(tg)
     sim = tg.Simulation(mesh, p, n, seed=rank, precision=32)
     sim.start()
     stream = torch.cuda.ExternalStream(sim.stream())
@@ -354,7 +354,7 @@ def run_ensemble(args):
     tg = importlib.import_module("2dtissue_gb300")
     ens = importlib.import_module("2dtissue_gb300.ensemble")
     mesh = tg.Mesh.ellipsoid(4, (4.0, 2.0, 2.0))
-    n, eta, v0 = ens.config3_replicas(seed=0, n_replicas=args.replicas)
+    n, eta, v0 = ens.ragged_replicas(seed=0, n_replicas=args.replicas)
     ps = [tg.Params(radius=0.05, r_max=0.12, v0=float(v), eta=float(e), dt=0.02) for e, v in zip(eta, v0)]
     sim = tg.Simulation(mesh, ps, [int(x) for x in n], seed=0, precision=32)
     sim.start()
@@ -502,10 +502,10 @@ def run_adjoint_batched(args):
 
 
 def run_profile(args):
-    """Minimal driver for ncu: the config-2 system, `warmup` steps, then `steps` steps; no timing."""
+    """Minimal driver for ncu: the 1M-particle system, `warmup` steps, then `steps` steps; no timing."""
     import torch
     tg = importlib.import_module("2dtissue_gb300")
-    mesh, p, n = config2(tg)
+    mesh, p, n = workload_1m(tg)
     sim = tg.Simulation(mesh, p, n, seed=0, precision=32)
     sim.start()
     sim.step(args.warmup)

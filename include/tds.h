@@ -136,7 +136,7 @@ int tds_sync(tds_sim* sim);
  * fixes its parameters in the _2DTissue constructor (2DTissue.h:37-54). */
 int tds_set_params(tds_sim* sim, const tds_params* params);
 
-/* ---- adjoint (no counterpart in the reference; SURVEY-planned entry point tds_adjoint_run) ----
+/* ---- adjoint (no counterpart in the reference, which has no derivatives) ----
  * Loss over a run of n_steps from the current state:
  *   L = w_pos * sum_r (1/N_r) sum_{i in r} |r_T,i - r*_i|^2  +  w_phi * sum_t sum_r (phi_t,r - phi*_t,r)^2
  * with r_T the 3D positions after the last step and phi_t the order parameter of step t. The
@@ -165,7 +165,8 @@ typedef struct tds_adjoint_result {
  * kernels per step. */
 int tds_adjoint_run(tds_sim* sim, const tds_adjoint_spec* spec, tds_adjoint_result* out);
 /* Per-kernel CUDA-event timing of directly launched steps (graphs are not used while enabled).
- * tds_kernel_times returns, per kernel (0 scan, 1 scatter, 2 order, 3 step, 4 finalize), the
+ * tds_kernel_times returns, per kernel (0 scan + order-parameter finalize, 1 scatter, 2 order, 3 step,
+ * 4 standalone finalize before a series read), the
  * summed device time in ms and the launch count since timing was enabled (arrays of 5). */
 int tds_kernel_timing(tds_sim* sim, int enable);
 int tds_kernel_times(tds_sim* sim, double* total_ms, long long* launches);

@@ -40,7 +40,7 @@ def get_mesh(tg, level, axes):
 
 @pytest.fixture(scope="session")
 def mesh_l4(tg):
-    """Config-1 mesh: level-4 icosphere scaled to the (2,1,1) ellipsoid."""
+    """Level-4 icosphere scaled to the (2,1,1) ellipsoid (the 100-particle system's mesh)."""
     return get_mesh(tg, 4, (2.0, 1.0, 1.0))
 
 

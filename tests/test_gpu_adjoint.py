@@ -75,7 +75,7 @@ def _start(tg, mesh, precision, params=None, n=N):
 
 @pytest.mark.parametrize("precision,n,rtol", [(64, N, 1e-6), (64, 200, 1e-8), (32, 200, 2e-3)])
 def test_adjoint_matches_dual_number_oracle(tg, orc, mesh_l4, adj_setup, precision, n, rtol):
-    """FP64: dense and sparse systems. FP32 on the sparse one (config-1 density), where an FP32
+    """FP64: dense and sparse systems. FP32 on the sparse one (the 100-particle system's density), where an FP32
     trajectory stays close to the FP64 one; in the dense system single particles reach
     sensitivities of 1e3-1e4 and FP32 and FP64 trajectories part."""
     N = n

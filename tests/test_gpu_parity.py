@@ -67,15 +67,15 @@ def compare_step(orc, om, params, g0, g1, step, seed, precision, subset=None, id
 
 
 @pytest.fixture(scope="module")
-def cfg1(tg, orc, mesh_l4):
+def sys100(tg, orc, mesh_l4):
     om, arr = oracle_mesh(orc, mesh_l4)
     return om, arr["v3"].mean(0)
 
 
 @pytest.mark.parametrize("precision", [64, 32])
-def test_config1_per_step_parity(tg, orc, mesh_l4, cfg1, precision):
-    """Config 1: (2,1,1) ellipsoid L4, 100 particles, 50 steps; each step checked."""
-    om, cen = cfg1
+def test_100_particle_per_step_parity(tg, orc, mesh_l4, sys100, precision):
+    """(2,1,1) ellipsoid L4, 100 particles, 50 steps; each step checked."""
+    om, cen = sys100
     p = tg.Params()
     sim = tg.Simulation(mesh_l4, p, 100, seed=0, precision=precision)
     sim.start()
@@ -92,9 +92,9 @@ def test_config1_per_step_parity(tg, orc, mesh_l4, cfg1, precision):
     assert sim.status() == 0
 
 
-def test_config1_denser_parity(tg, orc, mesh_l4, cfg1):
-    """2000 particles on the config-1 mesh (many neighbours, wraps, face changes), FP64 and FP32."""
-    om, cen = cfg1
+def test_2000_particle_parity(tg, orc, mesh_l4, sys100):
+    """2000 particles on the (2,1,1) ellipsoid mesh (many neighbours, wraps, face changes), FP64 and FP32."""
+    om, cen = sys100
     p = tg.Params()
     for precision in (64, 32):
         sim = tg.Simulation(mesh_l4, p, 2000, seed=5, precision=precision)
@@ -135,17 +135,17 @@ def test_seam_wrap_random_vs_oracle(tg, orc):
         assert abs(np.angle(np.exp(1j * (gth[i] - oth)))) < 1e-12 and gnw[i] == onw
 
 
-def config2_params(tg, mesh):
+def params_1m(tg, mesh):
     N = 1 << 20
     R = float(np.sqrt(0.5 * mesh.area / (np.pi * N)))
     return N, tg.Params(radius=R, r_max=2.4 * R, eta=0.3, dt=0.01)
 
 
-def test_config2_subset_parity(tg, orc):
-    """Config 2: (20,10,10) ellipsoid L7, 1,048,576 particles, FP32; the oracle gets the full state
+def test_1m_particle_subset_parity(tg, orc):
+    """(20,10,10) ellipsoid L7, 1,048,576 particles, FP32; the oracle gets the full state
     and updates a seeded subset of 4096 particles."""
     mesh = get_mesh(tg, 7, (20.0, 10.0, 10.0))
-    N, p = config2_params(tg, mesh)
+    N, p = params_1m(tg, mesh)
     om, arr = oracle_mesh(orc, mesh)
     sim = tg.Simulation(mesh, p, N, seed=2, precision=32)
     sim.start()
@@ -158,9 +158,9 @@ def test_config2_subset_parity(tg, orc):
     assert 1.0 < out["nbr"].mean() < 8.0
 
 
-def test_ensemble_parity(tg, orc, mesh_l4, cfg1):
+def test_ensemble_parity(tg, orc, mesh_l4, sys100):
     """Ragged ensemble: each replica matches the oracle run with that replica's parameters."""
-    om, cen = cfg1
+    om, cen = sys100
     ns = [64, 200, 1000, 37, 513]
     ps = [tg.Params(eta=e, v0=v) for e, v in zip([0.1, 2.0, 0.5, 6.0, 0.0], [0.5, 1.5, 1.0, 0.7, 1.2])]
     sim = tg.Simulation(mesh_l4, ps, ns, seed=4, precision=32)
@@ -239,8 +239,8 @@ def test_nonfinite_state_reports_status(tg, mesh_l4):
     assert sim.status() == 0
 
 
-def test_start_places_particles_on_the_surface(tg, orc, mesh_l4, cfg1):
-    om, _ = cfg1
+def test_start_places_particles_on_the_surface(tg, orc, mesh_l4, sys100):
+    om, _ = sys100
     sim = tg.Simulation(mesh_l4, tg.Params(), 5000, seed=12, precision=64)
     sim.start()
     s = sim.get_state()
@@ -250,9 +250,9 @@ def test_start_places_particles_on_the_surface(tg, orc, mesh_l4, cfg1):
     assert abs((s["r3d"][:, 0] < 0).mean() - 0.5) < 0.03
 
 
-def test_long_run_polar_order_statistics(tg, orc, mesh_l4, cfg1):
+def test_long_run_polar_order_statistics(tg, orc, mesh_l4, sys100):
     """Long-run polar order over 32 seeds: GPU FP32 and oracle FP64 means agree within 2 SE."""
-    om, cen = cfg1
+    om, cen = sys100
     p = tg.Params()
     g, o = [], []
     for seed in range(32):

@@ -21,7 +21,7 @@ def _worker(rank, world, port, q):
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     ens = importlib.import_module("2dtissue_gb300.ensemble")
-    n, eta, v0 = ens.config3_replicas(seed=3, n_replicas=257)
+    n, eta, v0 = ens.ragged_replicas(seed=3, n_replicas=257)
     shards = ens.shard_replicas(n, world)
     mine = shards[rank]
     # a stand-in per-replica series: replica index + step / 10, only for this rank's replicas
@@ -37,7 +37,7 @@ def _worker(rank, world, port, q):
 
 def test_shards_are_a_balanced_partition():
     ens = importlib.import_module("2dtissue_gb300.ensemble")
-    n, eta, v0 = ens.config3_replicas(seed=0)
+    n, eta, v0 = ens.ragged_replicas(seed=0)
     assert len(n) == 4096 and n.min() >= 64 and n.max() <= 8192
     assert 0 <= eta.min() and eta.max() <= 2 * np.pi and 0.5 <= v0.min() and v0.max() <= 1.5
     for world in (1, 2, 3, 8):
