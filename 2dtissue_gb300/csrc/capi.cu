@@ -565,6 +565,43 @@ int run_steps(tds_sim* s, int n, const double* noise_host, bool sync = true) {
     return TDS_OK;
 }
 
+// Device memory of one call (placement tables, adjoint buffers), released when it returns.
+struct Arena {
+    std::vector<void*> p;
+    ~Arena() {
+        for (void* q : p) cudaFree(q);
+    }
+    template <typename T>
+    T* get(size_t n) {
+        void* q = nullptr;
+        if (cudaMalloc(&q, std::max<size_t>(n * sizeof(T), 16)) != cudaSuccess) return nullptr;
+        p.push_back(q);
+        return (T*)q;
+    }
+};
+
+// Loads the state waiting in the input staging (k_load_state computes polarity, cell keys and
+// counts) on the compute stream; per-tile counts for the next scan.
+template <typename real>
+int load_from_staging(tds_sim* s, bool has_face, bool has_r3d, bool sync) {
+    const size_t N = (size_t)s->N;
+    s->cur = 0;
+    const int nb = (s->N + 255) / 256;
+    CK(cudaMemsetAsync(s->count, 0, (size_t)s->M * sizeof(int), s->stream));
+    CK(cudaMemsetAsync(s->tile_sum, 0, (size_t)2 * s->n_tiles * sizeof(int), s->stream));
+    tdsk::k_load_state<real><<<nb, 256, 0, s->stream>>>(
+        s->in_d, s->in_d + 2 * N, s->in_i, s->in_d + 3 * N, has_face, has_r3d, (const real*)s->rec, s->adj, s->G,
+        s->bin_start, s->bin_faces, s->packed_ids, (const RepParams<real>*)s->reps, s->local_bits, s->rows, s->ivals,
+        (R4<real>*)s->pos[0], (R4<real>*)s->pol[0], (R2<real>*)s->uv[0], s->ids[0], (R2<real>*)s->vel[0], s->cnt[0],
+        s->key[0], s->count, s->N, s->status);
+    tdsk::k_tile_sums<<<s->n_tiles, tdsk::kScanThreads, 0, s->stream>>>(s->count, s->M, s->tile_sum, s->n_tiles,
+                                                                         s->d_step);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(s->ev_in_free, s->stream));
+    if (sync) CK(cudaStreamSynchronize(s->stream));
+    return TDS_OK;
+}
+
 // Input: host -> input staging on the upload stream, then the load on the compute stream. The
 // upload waits until the previous load has consumed the staging.
 template <typename real>
@@ -587,21 +624,41 @@ int load_state(tds_sim* s, const tds_state_view* in, bool sync) {
     if (in->r3d) CK(cudaMemcpyAsync(d_r3, in->r3d, 3 * N * sizeof(double), cudaMemcpyHostToDevice, s->up));
     CK(cudaEventRecord(s->ev_in_ready, s->up));
     CK(cudaStreamWaitEvent(s->stream, s->ev_in_ready, 0));
-    s->cur = 0;
-    const int nb = (s->N + 255) / 256;
-    CK(cudaMemsetAsync(s->count, 0, (size_t)s->M * sizeof(int), s->stream));
-    CK(cudaMemsetAsync(s->tile_sum, 0, (size_t)2 * s->n_tiles * sizeof(int), s->stream));
-    tdsk::k_load_state<real><<<nb, 256, 0, s->stream>>>(
-        d_uv, d_th, d_face, d_r3, in->face != nullptr, in->r3d != nullptr, (const real*)s->rec, s->adj, s->G,
-        s->bin_start, s->bin_faces, s->packed_ids, (const RepParams<real>*)s->reps, s->local_bits, s->rows, s->ivals,
-        (R4<real>*)s->pos[0], (R4<real>*)s->pol[0], (R2<real>*)s->uv[0], s->ids[0], (R2<real>*)s->vel[0], s->cnt[0],
-        s->key[0], s->count, s->N, s->status);
-    tdsk::k_tile_sums<<<s->n_tiles, tdsk::kScanThreads, 0, s->stream>>>(s->count, s->M, s->tile_sum, s->n_tiles,
-                                                                         s->d_step);
+    return load_from_staging<real>(s, in->face != nullptr, in->r3d != nullptr, sync);
+}
+
+// Places particles on the device (k_place) into the input staging and loads them.
+template <typename real>
+int start_device(tds_sim* s) {
+    const tds::FaceTables& t = s->mesh->t;
+    const tds::Mesh& m = s->mesh->m;
+    const int F = t.F;
+    std::vector<double> pr((size_t)F * tdsk::kPlaceRec);
+    for (int f = 0; f < F; ++f) {
+        const double* r = &t.rec[(size_t)f * tds::kFaceRec];
+        double* d = &pr[(size_t)f * tdsk::kPlaceRec];
+        for (int k = 0; k < 6; ++k) d[k] = r[16 + k];     // uv corners
+        for (int k = 0; k < 3; ++k) d[6 + k] = r[24 + k];  // A
+        for (int k = 0; k < 6; ++k) d[9 + k] = r[k];       // J: column u, column v
+        for (int k = 0; k < 3; ++k) d[15 + k] = r[12 + k]; // normal
+        const int* t3 = &m.f3[3 * (size_t)f];
+        double e1[3], nrm = 0;
+        for (int k = 0; k < 3; ++k) e1[k] = m.v3[3 * (size_t)t3[1] + k] - m.v3[3 * (size_t)t3[0] + k], nrm += e1[k] * e1[k];
+        nrm = std::sqrt(nrm);
+        for (int k = 0; k < 3; ++k) d[18 + k] = e1[k] / nrm;
+    }
+    Arena A;
+    double* dpr = A.get<double>(pr.size());
+    double* dcdf = A.get<double>((size_t)F);
+    if (!dpr || !dcdf) return fail(s, TDS_ERR_NOMEM, "start: placement tables");
+    CK(cudaMemcpy(dpr, pr.data(), pr.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dcdf, t.area_cdf.data(), (size_t)F * sizeof(double), cudaMemcpyHostToDevice));
+    const size_t N = (size_t)s->N;
+    CK(cudaStreamWaitEvent(s->stream, s->ev_in_free, 0));
+    tdsk::k_place<<<(s->N + 255) / 256, 256, 0, s->stream>>>(dpr, dcdf, F, s->packed_ids, s->local_bits, s->seed,
+                                                              s->in_d, s->in_d + 2 * N, s->in_i, s->in_d + 3 * N, s->N);
     CK(cudaGetLastError());
-    CK(cudaEventRecord(s->ev_in_free, s->stream));
-    if (sync) CK(cudaStreamSynchronize(s->stream));
-    return TDS_OK;
+    return load_from_staging<real>(s, true, true, true);  // synchronises before the tables are freed
 }
 
 // Output: gather into the output staging on the compute stream, then device -> host on the
@@ -656,21 +713,6 @@ int sync_all(tds_sim* s) {
 // ---------------------------------------------------------------------------------------------
 // Adjoint run (tds_adjoint_run): forward with checkpoints, loss, reverse sweep
 // ---------------------------------------------------------------------------------------------
-// Device memory of one adjoint run, released when it returns.
-struct Arena {
-    std::vector<void*> p;
-    ~Arena() {
-        for (void* q : p) cudaFree(q);
-    }
-    template <typename T>
-    T* get(size_t n) {
-        void* q = nullptr;
-        if (cudaMalloc(&q, std::max<size_t>(n * sizeof(T), 16)) != cudaSuccess) return nullptr;
-        p.push_back(q);
-        return (T*)q;
-    }
-};
-
 // The input state of a step: buffer 0, the cell counts, the per-tile counts and the step counter.
 template <typename real>
 struct Snapshot {
@@ -1143,16 +1185,9 @@ int tds_ensemble_create(const tds_mesh* mesh, int n_replicas, const int* n_parti
 
 int tds_start(tds_sim* s) {
     if (!s) return TDS_ERR_ARG;
-    const size_t N = (size_t)s->N;
-    std::vector<double> uv(2 * N), th(N), r3(3 * N);
-    std::vector<int> fc(N);
-    for (int r = 0; r < s->R; ++r) {
-        const size_t o = (size_t)s->off[r];
-        tds::init_particles(s->mesh->m, s->mesh->t, s->n_rep[r], s->seed, (uint32_t)r, &uv[2 * o], &th[o], &fc[o],
-                            &r3[3 * o]);
-    }
-    tds_state_view v{uv.data(), th.data(), fc.data(), r3.data(), nullptr, nullptr};
-    return tds_set_state(s, &v);
+    int rc;
+    if ((rc = sync_all(s))) return rc;
+    return s->precision == 32 ? start_device<float>(s) : start_device<double>(s);
 }
 
 int tds_step(tds_sim* s, int n_steps, const double* noise) {

@@ -254,45 +254,5 @@ void build_cell_descriptors(const CellLevel& L, std::vector<uint32_t>& desc) {
     }
 }
 
-void init_particles(const Mesh& m, const FaceTables& t, int n, uint64_t seed, uint32_t rep, double* uv,
-                    double* theta, int* face, double* r3d) {
-    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
-    for (int i = 0; i < n; ++i) {
-        const uint32_t ctr[4] = {(uint32_t)i, rep, 0xFFFFFFFFu, 0u};
-        uint32_t o[4];
-        tdsr::philox10(ctr, key, o);
-        const double u1 = ((double)(o[0] >> 11) + 0.5) * (1.0 / 2097152.0);  // (0,1)
-        const double u2 = (double)(o[1] >> 8) * (1.0 / 16777216.0);
-        const double u3 = (double)(o[2] >> 8) * (1.0 / 16777216.0);
-        const double u4 = (double)(o[3] >> 8) * (1.0 / 16777216.0);
-        int f = (int)(std::lower_bound(t.area_cdf.begin(), t.area_cdf.end(), u1) - t.area_cdf.begin());
-        f = std::min(f, t.F - 1);
-        const double* r = &t.rec[(size_t)f * kFaceRec];
-        const double s2 = std::sqrt(u2);
-        const double w0 = 1.0 - s2, w1 = s2 * (1.0 - u3), w2 = s2 * u3;
-        double pu = w0 * r[16] + w1 * r[18] + w2 * r[20];
-        double pv = w0 * r[17] + w1 * r[19] + w2 * r[21];
-        uv[2 * i] = pu, uv[2 * i + 1] = pv;
-        face[i] = f;
-        const double du = pu - r[16], dv = pv - r[17];
-        for (int k = 0; k < 3; ++k) r3d[3 * i + k] = r[24 + k] + r[k] * du + r[3 + k] * dv;
-        // face frame: e1 along B - A, e2 = n x e1
-        const int* t3 = &m.f3[3 * f];
-        double e1[3], nrm = 0;
-        for (int k = 0; k < 3; ++k) e1[k] = m.v3[3 * t3[1] + k] - m.v3[3 * t3[0] + k], nrm += e1[k] * e1[k];
-        nrm = std::sqrt(nrm);
-        for (int k = 0; k < 3; ++k) e1[k] /= nrm;
-        const double* nn = &r[12];
-        const double e2[3] = {nn[1] * e1[2] - nn[2] * e1[1], nn[2] * e1[0] - nn[0] * e1[2],
-                              nn[0] * e1[1] - nn[1] * e1[0]};
-        const double phi = 6.28318530717958647692 * u4;
-        const double cp = std::cos(phi), sp = std::sin(phi);
-        double p[3];
-        for (int k = 0; k < 3; ++k) p[k] = cp * e1[k] + sp * e2[k];
-        const double w_u = r[6] * p[0] + r[7] * p[1] + r[8] * p[2];
-        const double w_v = r[9] * p[0] + r[10] * p[1] + r[11] * p[2];
-        theta[i] = std::atan2(w_v, w_u);
-    }
-}
 
 }  // namespace tds

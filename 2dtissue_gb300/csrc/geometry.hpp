@@ -57,11 +57,6 @@ void build_cell_level(const Mesh& m, double h, const double origin[3], CellLevel
 // skips a non-surface cell. 12 words per cell (2 spare).
 void build_cell_descriptors(const CellLevel& L, std::vector<uint32_t>& desc);
 
-// Seeded placement: face picked with probability proportional to its 3D area, uniform
-// barycentric position, polarity angle uniform in [0, 2pi) in the face frame
-// (e1 = normalize(B - A), e2 = n x e1), expressed as a chart angle.
-void init_particles(const Mesh& m, const FaceTables& t, int n, uint64_t seed, uint32_t rep, double* uv,
-                    double* theta, int* face, double* r3d);
 
 // Host Philox4x32-10 (same generator as the device), for placement draws.
 void philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

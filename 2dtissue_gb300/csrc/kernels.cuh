@@ -939,6 +939,63 @@ __global__ void k_load_state(const double* i_uv, const double* i_th, const int* 
     atomicAdd(&count[k], 1);
 }
 
+// Seeded placement on the device (FP64): face drawn with probability proportional to its 3D area
+// (lower bound of u1 in the area CDF), uniform barycentric point (sqrt(u2), u3), polarity at angle
+// 2 pi u4 from e1 = normalize(B - A) in the face's tangent frame (e2 = n x e1), as a chart angle.
+// Draws: Philox4x32-10(ctr = (local index, replica, 0xFFFFFFFF, 0), key = seed), the same stream
+// as the host placement. Face data per face: uv corners a, b, c (6), A (3), J (6, column u then
+// v), n (3), e1 (3) = kPlaceRec doubles. Output in id order into the state-load staging.
+constexpr int kPlaceRec = 21;
+__global__ void k_place(const double* __restrict__ frec, const double* __restrict__ cdf, int F,
+                        const int* __restrict__ packed_ids, int local_bits, unsigned long long seed, double* o_uv,
+                        double* o_th, int* o_face, double* o_r3d, int N) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const unsigned id = (unsigned)packed_ids[i];
+    const uint32_t ctr[4] = {id & ((1u << local_bits) - 1u), id >> local_bits, 0xFFFFFFFFu, 0u};
+    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    uint32_t o[4];
+    tdsr::philox10(ctr, key, o);
+    const double u1 = __dmul_rn(__dadd_rn((double)(o[0] >> 11), 0.5), 1.0 / 2097152.0);  // (0, 1)
+    const double u2 = __dmul_rn((double)(o[1] >> 8), 1.0 / 16777216.0);
+    const double u3 = __dmul_rn((double)(o[2] >> 8), 1.0 / 16777216.0);
+    const double u4 = __dmul_rn((double)(o[3] >> 8), 1.0 / 16777216.0);
+    int lo = 0, hi = F;  // first face with cdf >= u1
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (cdf[mid] < u1)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    const int f = min(lo, F - 1);
+    const double* r = frec + (size_t)f * kPlaceRec;
+    const double s2 = sqrt(u2);
+    const double w0 = __dadd_rn(1.0, -s2), w1 = __dmul_rn(s2, __dadd_rn(1.0, -u3)), w2 = __dmul_rn(s2, u3);
+    const double pu = __dadd_rn(__dadd_rn(__dmul_rn(w0, r[0]), __dmul_rn(w1, r[2])), __dmul_rn(w2, r[4]));
+    const double pv = __dadd_rn(__dadd_rn(__dmul_rn(w0, r[1]), __dmul_rn(w1, r[3])), __dmul_rn(w2, r[5]));
+    o_uv[2 * (size_t)i] = pu, o_uv[2 * (size_t)i + 1] = pv;
+    o_face[i] = f;
+    const double du = __dadd_rn(pu, -r[0]), dv = __dadd_rn(pv, -r[1]);
+    for (int k = 0; k < 3; ++k)
+        o_r3d[3 * (size_t)i + k] = __dadd_rn(__dadd_rn(r[6 + k], __dmul_rn(r[9 + k], du)), __dmul_rn(r[12 + k], dv));
+    const double* n = r + 15;
+    const double* e1 = r + 18;
+    const double e2[3] = {__dadd_rn(__dmul_rn(n[1], e1[2]), -__dmul_rn(n[2], e1[1])),
+                          __dadd_rn(__dmul_rn(n[2], e1[0]), -__dmul_rn(n[0], e1[2])),
+                          __dadd_rn(__dmul_rn(n[0], e1[1]), -__dmul_rn(n[1], e1[0]))};
+    double sp, cp;
+    sincos(__dmul_rn(6.28318530717958647692, u4), &sp, &cp);
+    double p[3];
+    for (int k = 0; k < 3; ++k) p[k] = __dadd_rn(__dmul_rn(cp, e1[k]), __dmul_rn(sp, e2[k]));
+    // chart direction through the pseudo-inverse of J
+    const double ux = r[9], uy = r[10], uz = r[11], vx = r[12], vy = r[13], vz = r[14];
+    const double g11 = ux * ux + uy * uy + uz * uz, g12 = ux * vx + uy * vy + uz * vz, g22 = vx * vx + vy * vy + vz * vz;
+    const double pu3 = ux * p[0] + uy * p[1] + uz * p[2], pv3 = vx * p[0] + vy * p[1] + vz * p[2];
+    const double wu = g22 * pu3 - g12 * pv3, wv = g11 * pv3 - g12 * pu3;  // (J^T J)^-1 J^T p times det > 0
+    o_th[i] = atan2(wv, wu);
+}
+
 template <typename real>
 __global__ void k_debug_wrap(int n, const double* uv_old, double* uv, double* th, double* vel, int* nw_out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
