@@ -53,6 +53,11 @@ class _AdjResult(C.Structure):
 GRAD_PARAMS = ("k_rep", "k_adh", "v0", "mu", "tau", "align", "eta")
 
 
+class _Tuning(C.Structure):
+    _fields_ = [("cells_per_particle", C.c_double), ("step_block", C.c_int), ("graph_steps", C.c_int),
+                ("reserved", C.c_int)]
+
+
 class _StateView(C.Structure):
     _fields_ = [("uv", C.c_void_p), ("theta", C.c_void_p), ("face", C.c_void_p), ("r3d", C.c_void_p),
                 ("vel_uv", C.c_void_p), ("nbr_count", C.c_void_p)]
@@ -95,6 +100,9 @@ def lib(build_if_missing=True):
     L.tds_get_state_async.argtypes = [VP, P(_StateView)]
     L.tds_sync.argtypes = [VP]
     L.tds_set_params.argtypes = [VP, VP]
+    L.tds_create_ex.argtypes = [VP, I, VP, VP, C.c_uint64, I, P(_Tuning), P(VP)]
+    L.tds_get_tuning.argtypes = [VP, P(_Tuning)]
+    L.tds_autotune.argtypes = [VP, I, VP, VP, C.c_uint64, I, I, P(_Tuning), P(D)]
     L.tds_adjoint_run.argtypes = [VP, P(_AdjSpec), P(_AdjResult)]
     L.tds_get_order_parameter.argtypes = [VP, VP, VP, I, P(I)]
     L.tds_get_step.argtypes = [VP, P(C.c_int64)]
@@ -203,12 +211,20 @@ class Mesh:
 class Simulation:
     """One system (n_particles int) or a ragged ensemble (n_particles list, params list)."""
 
-    def __init__(self, mesh, params, n_particles, seed=0, precision=32):
+    def __init__(self, mesh, params, n_particles, seed=0, precision=32, tuning=None):
         self.mesh = mesh
         self._pending = []  # host arrays of enqueued transfers, held until sync()
         L = lib()
         h = C.c_void_p()
-        if np.ndim(n_particles) == 0:
+        if tuning is not None:
+            n = np.atleast_1d(np.ascontiguousarray(n_particles, np.int32))
+            ps = list(params) if isinstance(params, (list, tuple)) else [params] * len(n)
+            self.params = ps
+            arr = (_Params * len(n))(*[q.to_c() for q in ps])
+            t = _Tuning(float(tuning["cells_per_particle"]), int(tuning["step_block"]), int(tuning["graph_steps"]), 0)
+            rc = L.tds_create_ex(mesh.h, len(n), n.ctypes.data, C.cast(arr, C.c_void_p), C.c_uint64(seed),
+                                 int(precision), C.byref(t), C.byref(h))
+        elif np.ndim(n_particles) == 0:
             self.params = [params]
             p = params.to_c()
             rc = L.tds_create(mesh.h, C.byref(p), int(n_particles), C.c_uint64(seed), int(precision), C.byref(h))
@@ -304,6 +320,11 @@ class Simulation:
             self._check(lib().tds_sync(self.h))
         finally:
             self._pending = []
+
+    def tuning(self):
+        t = _Tuning()
+        self._check(lib().tds_get_tuning(self.h, C.byref(t)))
+        return dict(cells_per_particle=t.cells_per_particle, step_block=t.step_block, graph_steps=t.graph_steps)
 
     def set_params(self, params):
         """New model parameters (one Params, or one per replica); radius and r_max must not change."""
@@ -417,6 +438,19 @@ class Tissue:
     def get_order_parameter(self):
         phi, _ = self.sim.order_parameter()
         return phi[:, 0]
+
+
+def autotune(mesh, params, n_particles, seed=0, precision=32, trial_steps=64):
+    """Times each candidate tuning on this workload; returns (tuning dict, particle-steps/s)."""
+    n = np.atleast_1d(np.ascontiguousarray(n_particles, np.int32))
+    ps = list(params) if isinstance(params, (list, tuple)) else [params] * len(n)
+    arr = (_Params * len(n))(*[q.to_c() for q in ps])
+    t, rate = _Tuning(), C.c_double()
+    rc = lib().tds_autotune(mesh.h, len(n), n.ctypes.data, C.cast(arr, C.c_void_p), C.c_uint64(seed), int(precision),
+                            int(trial_steps), C.byref(t), C.byref(rate))
+    if rc != TDS_OK:
+        raise TdsError(rc, "autotune failed")
+    return dict(cells_per_particle=t.cells_per_particle, step_block=t.step_block, graph_steps=t.graph_steps), rate.value
 
 
 def debug_seam_wrap(uv_old, uv, theta=None, vel=None, precision=64):

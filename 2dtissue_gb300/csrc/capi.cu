@@ -109,7 +109,9 @@ struct tds_sim {
     cudaEvent_t ev_in_ready = nullptr, ev_in_free = nullptr, ev_out_ready = nullptr, ev_out_free = nullptr;
     int cur = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    int graph_steps = 16;
+    int graph_steps = 16;        // steps per captured CUDA graph (tuning; even)
+    int step_block = 256;        // threads per k_step block (tuning: 128 or 256)
+    double cells_per_particle = 4.0;  // cell-level rule (tuning): finest level with C <= max(64, this * N_r)
     double origin[3] = {0, 0, 0};
     std::vector<void*> allocs;
     // per-kernel event timing
@@ -227,7 +229,7 @@ int upload_tables(tds_sim* s) {
         int li = 0;
         for (int k = 0; k <= 6; ++k) {
             li = get_level(s->prm[r].r_max, k);
-            if (levels[li].L.C <= std::max(64, 4 * s->n_rep[r])) break;
+            if ((double)levels[li].L.C <= std::max(64.0, s->cells_per_particle * s->n_rep[r])) break;
         }
         s->level_of[r] = li;
     }
@@ -505,10 +507,12 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
     a.seed = s->seed;
     a.status = s->status;
     a.N = s->N;
-    const int ns = (s->N + tdsk::kStepThreads - 1) / tdsk::kStepThreads;
     {
         KernelTimer kt(s, 3);
-        tdsk::k_step<real><<<ns, tdsk::kStepThreads, 0, st>>>(a);
+        if (s->step_block == 128)
+            tdsk::k_step<real, 128><<<(s->N + 127) / 128, 128, 0, st>>>(a);
+        else
+            tdsk::k_step<real, 256><<<(s->N + 255) / 256, 256, 0, st>>>(a);
     }
 }
 
@@ -1040,7 +1044,7 @@ int check_params(const tds_params& p, std::string& why) {
 }
 
 int create_impl(const tds_mesh* mesh, int R, const int* n, const tds_params* prm, uint64_t seed, int precision,
-                tds_sim** out) {
+                tds_sim** out, const tds_tuning* tune = nullptr) {
     if (!out) return TDS_ERR_ARG;
     *out = nullptr;
     auto s = std::make_unique<tds_sim>();
@@ -1051,6 +1055,14 @@ int create_impl(const tds_mesh* mesh, int R, const int* n, const tds_params* prm
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return TDS_ERR_CUDA;
     s->mesh = mesh;
     s->precision = precision;
+    if (tune) {
+        if (!(tune->cells_per_particle > 0) || (tune->step_block != 128 && tune->step_block != 256) ||
+            tune->graph_steps < 2 || tune->graph_steps % 2 || tune->graph_steps > 256)
+            return TDS_ERR_ARG;
+        s->cells_per_particle = tune->cells_per_particle;
+        s->step_block = tune->step_block;
+        s->graph_steps = tune->graph_steps;
+    }
     s->rsz = precision == 32 ? 4 : 8;
     s->R = R;
     s->seed = seed;
@@ -1181,6 +1193,63 @@ int tds_ensemble_create(const tds_mesh* mesh, int n_replicas, const int* n_parti
                         uint64_t seed, int precision, tds_sim** out) {
     if (!n_particles || !params) return TDS_ERR_ARG;
     return create_impl(mesh, n_replicas, n_particles, params, seed, precision, out);
+}
+
+int tds_create_ex(const tds_mesh* mesh, int n_replicas, const int* n_particles, const tds_params* params,
+                  uint64_t seed, int precision, const tds_tuning* tuning, tds_sim** out) {
+    if (!n_particles || !params) return TDS_ERR_ARG;
+    return create_impl(mesh, n_replicas, n_particles, params, seed, precision, out, tuning);
+}
+
+int tds_get_tuning(const tds_sim* s, tds_tuning* out) {
+    if (!s || !out) return TDS_ERR_ARG;
+    out->cells_per_particle = s->cells_per_particle;
+    out->step_block = s->step_block;
+    out->graph_steps = s->graph_steps;
+    return TDS_OK;
+}
+
+int tds_autotune(const tds_mesh* mesh, int n_replicas, const int* n_particles, const tds_params* params,
+                 uint64_t seed, int precision, int trial_steps, tds_tuning* best, double* best_rate) {
+    if (!mesh || !n_particles || !params || !best || trial_steps < 1) return TDS_ERR_ARG;
+    // candidates: the cell-level rule, the step block and the graph chunk; each is timed on the
+    // caller's workload (created, placed, warmed up, then trial_steps graph-launched steps)
+    const double cpp[] = {1.0, 4.0, 16.0};
+    const int blocks[] = {128, 256};
+    const int chunks[] = {16, 32};
+    double best_r = -1;
+    tds_tuning bt{4.0, 256, 16, 0};
+    long long total = 0;
+    for (int r = 0; r < n_replicas; ++r) total += n_particles[r];
+    for (double c : cpp)
+        for (int b : blocks)
+            for (int g : chunks) {
+                tds_tuning t{c, b, g, 0};
+                tds_sim* s = nullptr;
+                int rc = create_impl(mesh, n_replicas, n_particles, params, seed, precision, &s, &t);
+                if (rc) return rc;
+                cudaEvent_t e0 = nullptr, e1 = nullptr;
+                float ms = 0;
+                rc = tds_start(s);
+                if (!rc) rc = tds_step(s, g, nullptr);  // warm-up: graph capture
+                if (!rc && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
+                    cudaEventRecord(e0, s->stream);
+                    rc = tds_step_async(s, (trial_steps + g - 1) / g * g);
+                    cudaEventRecord(e1, s->stream);
+                    if (!rc) rc = tds_sync(s);
+                    if (!rc) cudaEventElapsedTime(&ms, e0, e1);
+                }
+                if (e0) cudaEventDestroy(e0);
+                if (e1) cudaEventDestroy(e1);
+                const int steps = (trial_steps + g - 1) / g * g;
+                tds_destroy(s);
+                if (rc) return rc;
+                const double rate = ms > 0 ? (double)total * steps / (ms * 1e-3) : 0.0;
+                if (rate > best_r) best_r = rate, bt = t;
+            }
+    *best = bt;
+    if (best_rate) *best_rate = best_r;
+    return TDS_OK;
 }
 
 int tds_start(tds_sim* s) {

@@ -51,7 +51,7 @@ constexpr int kMaxWraps = 8;      // seam wraps per particle per step
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 32;
 constexpr int kScanTile = kScanThreads * kScanItems;  // buckets per scan tile
-constexpr int kStepThreads = 256;
+constexpr int kStepThreads = 256;  // default block of k_step
 constexpr int kPhiCopies = 32;    // spread the order-parameter atomics over copies
 
 template <typename real>
@@ -427,10 +427,12 @@ __device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<re
     }
 }
 
-template <typename real>
-__global__ void __launch_bounds__(kStepThreads, sizeof(real) == 4 ? 5 : 3) k_step(const StepArgs<real> a) {
+// BLOCK: threads per block (a tuning choice: 128 or 256); the register budget is the same either
+// way (5 blocks of 256, 10 of 128 per SM in FP32).
+template <typename real, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 5 : 3) * 256 / BLOCK) k_step(const StepArgs<real> a) {
     typedef R4<real> r4;
-    const int q = blockIdx.x * kStepThreads + threadIdx.x;
+    const int q = blockIdx.x * BLOCK + threadIdx.x;
     const bool active = q < a.N;
     int rep = -1;
     real ph[6] = {0, 0, 0, 0, 0, 0};

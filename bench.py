@@ -356,7 +356,10 @@ def run_ensemble(args):
     mesh = tg.Mesh.ellipsoid(4, (4.0, 2.0, 2.0))
     n, eta, v0 = ens.ragged_replicas(seed=0, n_replicas=args.replicas)
     ps = [tg.Params(radius=0.05, r_max=0.12, v0=float(v), eta=float(e), dt=0.02) for e, v in zip(eta, v0)]
-    sim = tg.Simulation(mesh, ps, [int(x) for x in n], seed=0, precision=32)
+    tuning, tune_rate = None, None
+    if args.autotune:
+        tuning, tune_rate = tg.autotune(mesh, ps, [int(x) for x in n], seed=0, precision=32, trial_steps=32)
+    sim = tg.Simulation(mesh, ps, [int(x) for x in n], seed=0, precision=32, tuning=tuning)
     sim.start()
     stream = torch.cuda.ExternalStream(sim.stream())
     sim.step(max(args.warmup, 3))
@@ -369,6 +372,7 @@ def run_ensemble(args):
     assert sim.status() == 0
     batched = int(n.sum()) * args.steps / (a.elapsed_time(b) * 1e-3)
     phi, psi = sim.order_parameter()
+    sim_tuning = sim.tuning()
     sim.close()
     # one by one: a seeded sample of replicas, each its own plain handle
     sample = np.sort(np.random.default_rng(1).choice(len(n), min(args.sample, len(n)), replace=False))
@@ -394,6 +398,7 @@ def run_ensemble(args):
                                                   "replicas": len(n), "particles": int(n.sum()),
                                                   "l2": "inputs larger than L2 (no flush)"},
             "one_by_one": {"value": one_by_one, "replicas_sampled": len(sample), "steps": steps1},
+            "tuning": sim_tuning, "autotuned": bool(args.autotune),
             "batched_over_one_by_one": batched / one_by_one,
             "order_parameter_series": {"steps": int(phi.shape[0]), "replicas": int(phi.shape[1]),
                                        "mean_phi_last": float(phi[-1].mean())}}
@@ -526,6 +531,7 @@ def main():
     ap.add_argument("--workload", default="plain", choices=["plain", "ensemble", "adjoint", "adjoint_batched"])
     ap.add_argument("--replicas", type=int, default=4096, help="ensemble workload: replicas")
     ap.add_argument("--sample", type=int, default=256, help="ensemble workload: replicas run one by one")
+    ap.add_argument("--autotune", action="store_true", help="ensemble workload: time the autotuner's choice")
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)

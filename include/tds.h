@@ -88,6 +88,28 @@ int tds_create(const tds_mesh* mesh, const tds_params* params, int n_particles, 
 /* Ragged ensemble of independent replicas in one set of launches; params has n_replicas entries. */
 int tds_ensemble_create(const tds_mesh* mesh, int n_replicas, const int* n_particles, const tds_params* params,
                         uint64_t seed, int precision, tds_sim** out);
+/* ---- tuning (no counterpart in the reference) ----
+ * cells_per_particle: a replica's cell size is r_max * 2^k for the smallest k whose surface-cell
+ *   count is <= max(64, cells_per_particle * N_r) (small replicas on a large surface take
+ *   coarser cells); default 4.
+ * step_block: threads per block of the step kernel, 128 or 256 (default 256).
+ * graph_steps: steps per captured CUDA graph, even, 2..256 (default 16). */
+typedef struct tds_tuning {
+    double cells_per_particle;
+    int step_block;
+    int graph_steps;
+    int reserved;
+} tds_tuning;
+/* tds_ensemble_create with a tuning (NULL = defaults); n_replicas = 1 for a plain system. */
+int tds_create_ex(const tds_mesh* mesh, int n_replicas, const int* n_particles, const tds_params* params,
+                  uint64_t seed, int precision, const tds_tuning* tuning, tds_sim** out);
+int tds_get_tuning(const tds_sim* sim, tds_tuning* out);
+/* Autotuner: creates the workload with each candidate tuning (cells_per_particle 1, 4, 16 x
+ * step_block 128, 256 x graph_steps 16, 32), places it, and times trial_steps graph-launched steps
+ * on the device; returns the fastest tuning and its particle-steps/s. */
+int tds_autotune(const tds_mesh* mesh, int n_replicas, const int* n_particles, const tds_params* params,
+                 uint64_t seed, int precision, int trial_steps, tds_tuning* best, double* best_rate);
+
 /* Area-weighted random placement, polarity uniform in the face tangent frame (Philox, seeded). */
 int tds_start(tds_sim* sim);
 /* n_steps of the update. noise: NULL (Philox noise) or n_steps x N angle increments in id order. */

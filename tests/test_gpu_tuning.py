@@ -1,0 +1,57 @@
+"""Tuning choices (tds_create_ex) and the autotuner (tds_autotune): the step block changes no
+bit; a coarser cell level keeps per-step parity with the oracle; the autotuner returns one of its
+candidates with a positive rate."""
+import numpy as np
+import pytest
+
+from conftest import oracle_mesh
+from test_gpu_parity import compare_step
+
+pytestmark = pytest.mark.gpu
+
+
+def test_step_block_changes_no_bit(tg, mesh_l4):
+    outs = []
+    for b in (128, 256):
+        sim = tg.Simulation(mesh_l4, tg.Params(), 3000, seed=4, tuning=dict(cells_per_particle=4.0, step_block=b,
+                                                                            graph_steps=16))
+        assert sim.tuning()["step_block"] == b
+        sim.start()
+        sim.step(37)
+        outs.append(sim.get_state())
+    for k in outs[0]:
+        np.testing.assert_array_equal(outs[0][k], outs[1][k])
+
+
+@pytest.mark.parametrize("cpp", [0.25, 64.0])
+def test_cell_level_rule_keeps_parity(tg, orc, mesh_l4, cpp):
+    """Ragged replicas with a coarse (0.25 cells per particle) and a fine (64) cell-level rule."""
+    om, arr = oracle_mesh(orc, mesh_l4)
+    cen = arr["v3"].mean(0)
+    ns = [64, 300, 1000]
+    sim = tg.Simulation(mesh_l4, [tg.Params()] * 3, ns, seed=6, precision=64,
+                        tuning=dict(cells_per_particle=cpp, step_block=256, graph_steps=16))
+    sim.start()
+    sim.step(3)
+    g0 = sim.get_state()
+    sim.step(1)
+    g1 = sim.get_state()
+    lb = int(np.ceil(np.log2(max(ns))))
+    off = np.concatenate([[0], np.cumsum(ns)])
+    for r, n in enumerate(ns):
+        sl = slice(off[r], off[r + 1])
+        a = {k: v[sl] for k, v in g0.items()}
+        b = {k: v[sl] for k, v in g1.items()}
+        ids = ((r << lb) | np.arange(n)).astype(np.int32)
+        compare_step(orc, om, tg.Params().oracle_dict(), a, b, 3, 6, 64, ids=ids, local_bits=lb, centroid=cen)
+
+
+def test_autotune_returns_a_candidate(tg, mesh_l4):
+    ns = [200, 800, 3000]
+    t, rate = tg.autotune(mesh_l4, [tg.Params()] * 3, ns, trial_steps=32)
+    assert t["cells_per_particle"] in (1.0, 4.0, 16.0) and t["step_block"] in (128, 256)
+    assert t["graph_steps"] in (16, 32) and rate > 0
+    sim = tg.Simulation(mesh_l4, [tg.Params()] * 3, ns, tuning=t)
+    sim.start()
+    sim.step(t["graph_steps"])
+    assert sim.status() == 0
