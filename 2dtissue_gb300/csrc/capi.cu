@@ -507,6 +507,12 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
     a.seed = s->seed;
     a.status = s->status;
     a.N = s->N;
+    a.single = s->R == 1;
+    {
+        const RepParams<real>& r0 = *(const RepParams<real>*)s->reps_host.data();
+        a.pc0.r_max2 = r0.r_max2, a.pc0.twoR = r0.twoR, a.pc0.inv_twoR = r0.inv_twoR, a.pc0.k = r0.k;
+        a.pc0.adh_scale = r0.adh_scale;
+    }
     {
         KernelTimer kt(s, 3);
         if (s->step_block == 128)
@@ -956,6 +962,7 @@ int set_params(tds_sim* s, const tds_params* prm) {
     CK(cudaMemcpy(s->reps, rp.data(), rp.size() * sizeof(RepParams<real>), cudaMemcpyHostToDevice));
     s->reps_host.assign((const unsigned char*)rp.data(), (const unsigned char*)(rp.data() + rp.size()));
     for (int r = 0; r < s->R; ++r) s->prm[r] = prm[r];
+    free_graphs(s);  // captured launches carry the single-replica pair constants
     return TDS_OK;
 }
 

@@ -78,6 +78,12 @@ struct RepParams {
                                           // desc_off: the level's descriptor offset (uint4 units)
 };
 
+// The constants of the pair force (a replica's).
+template <typename real>
+struct PairC {
+    real r_max2, twoR, inv_twoR, k, adh_scale;
+};
+
 template <typename real>
 struct StepArgs {
     const R4<real>* pos;  // state in sorted order (k_order output)
@@ -114,6 +120,8 @@ struct StepArgs {
     unsigned long long seed;
     int* status;
     int N;
+    int single;  // one replica: pc0 holds its pair constants
+    PairC<real> pc0;
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -404,7 +412,14 @@ __device__ __forceinline__ void add_tile(int* tile_sum, int key) {
 // ---------------------------------------------------------------------------------------------
 // One neighbour candidate: 3D chord distance test, Szabo force and polarity sums.
 template <typename real>
-__device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<real>& P, const R4<real>& Q,
+__device__ __forceinline__ PairC<real> pair_constants(const RepParams<real>& rp) {
+    PairC<real> c;
+    c.r_max2 = rp.r_max2, c.twoR = rp.twoR, c.inv_twoR = rp.inv_twoR, c.k = rp.k, c.adh_scale = rp.adh_scale;
+    return c;
+}
+
+template <typename real>
+__device__ __forceinline__ void pair_term(const PairC<real>& rp, const R4<real>& P, const R4<real>& Q,
                                           const R4<real>* __restrict__ pol, int j, bool self, real (&acc)[6],
                                           int& cnt) {
     const real dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
@@ -424,6 +439,44 @@ __device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<re
         acc[4] += QL.y;
         acc[5] += QL.z;
         ++cnt;
+    }
+}
+template <typename real>
+__device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<real>& P, const R4<real>& Q,
+                                          const R4<real>* __restrict__ pol, int j, bool self, real (&acc)[6],
+                                          int& cnt) {
+    pair_term(pair_constants(rp), P, Q, pol, j, self, acc, cnt);
+}
+
+// Pair sums over a particle's candidate runs in a fixed order (runs 0..8, slots ascending), two
+// candidates per iteration.
+template <typename real>
+__device__ __forceinline__ void pair_sums(const PairC<real>& pc, const R4<real>& P, const R4<real>* __restrict__ pos,
+                                          const R4<real>* __restrict__ pol, const int2 (&run)[9], int total, int self,
+                                          real (&acc)[6], int& cnt) {
+    int r = 0, t = run[0].x, left = run[0].y;
+    for (int k = 0; k < total; k += 2) {
+        while (left == 0) {
+            const int2 x = run[++r];
+            t = x.x;
+            left = x.y;
+        }
+        const int ta = t++;
+        --left;
+        int tb = -1;
+        if (k + 1 < total) {
+            while (left == 0) {
+                const int2 x = run[++r];
+                t = x.x;
+                left = x.y;
+            }
+            tb = t++;
+            --left;
+        }
+        const R4<real> Qa = pos[ta];
+        const R4<real> Qb = pos[tb >= 0 ? tb : ta];
+        pair_term(pc, P, Qa, pol, ta, ta == self, acc, cnt);
+        if (tb >= 0) pair_term(pc, P, Qb, pol, tb, tb == self, acc, cnt);
     }
 }
 
@@ -473,33 +526,15 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 5 : 3) * 256 / BLO
 #pragma unroll
             for (int r = 0; r < 9; ++r) run[r] = make_int2(0, 0);
         }
-        // pair sums over all candidates (in a fixed order), two per iteration
+        // pair sums over all candidates (in a fixed order); a single-replica system takes the
+        // pair constants from the kernel parameters (constant bank) rather than from the replica
+        // table, so the loop does not re-read them from global memory
         real acc[6] = {0, 0, 0, 0, 0, 0};
         int cnt = 0;
-        int r = 0, t = run[0].x, left = run[0].y;
-        for (int k = 0; k < total; k += 2) {
-            while (left == 0) {
-                const int2 x = run[++r];
-                t = x.x;
-                left = x.y;
-            }
-            const int ta = t++;
-            --left;
-            int tb = -1;
-            if (k + 1 < total) {
-                while (left == 0) {
-                    const int2 x = run[++r];
-                    t = x.x;
-                    left = x.y;
-                }
-                tb = t++;
-                --left;
-            }
-            const r4 Qa = a.pos[ta];
-            const r4 Qb = a.pos[tb >= 0 ? tb : ta];
-            pair_term(rp, P, Qa, a.pol, ta, ta == q, acc, cnt);
-            if (tb >= 0) pair_term(rp, P, Qb, a.pol, tb, tb == q, acc, cnt);
-        }
+        if (a.single)
+            pair_sums(a.pc0, P, a.pos, a.pol, run, total, q, acc, cnt);
+        else
+            pair_sums(pair_constants(rp), P, a.pos, a.pol, run, total, q, acc, cnt);
         const real Fxr = acc[0], Fyr = acc[1], Fzr = acc[2];
         const real mxr = acc[3], myr = acc[4], mzr = acc[5];
 
