@@ -58,6 +58,10 @@ class _Tuning(C.Structure):
                 ("reserved", C.c_int)]
 
 
+class _RefParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("v0", "k", "sigma", "r_adh", "k_adh", "step_size")]
+
+
 class _StateView(C.Structure):
     _fields_ = [("uv", C.c_void_p), ("theta", C.c_void_p), ("face", C.c_void_p), ("r3d", C.c_void_p),
                 ("vel_uv", C.c_void_p), ("nbr_count", C.c_void_p)]
@@ -118,6 +122,17 @@ def lib(build_if_missing=True):
     L.tds_last_error.restype = C.c_char_p
     L.tds_destroy.argtypes = [VP]
     L.tds_debug_seam_wrap.argtypes = [I, VP, VP, VP, VP, VP, I]
+    L.tds_ref_vertex_distances.argtypes = [VP, VP]
+    L.tds_ref_create.argtypes = [VP, VP, P(_RefParams), I, C.c_uint64, P(VP)]
+    L.tds_ref_start.argtypes = [VP]
+    L.tds_ref_set_state.argtypes = [VP, VP, VP, VP]
+    L.tds_ref_step.argtypes = [VP, I]
+    L.tds_ref_get_state.argtypes = [VP, VP, VP, VP, VP, VP, VP]
+    L.tds_ref_get_order_parameter.argtypes = [VP, VP, I, P(I)]
+    L.tds_ref_stream.argtypes = [VP, P(VP)]
+    L.tds_ref_last_error.argtypes = [VP]
+    L.tds_ref_last_error.restype = C.c_char_p
+    L.tds_ref_destroy.argtypes = [VP]
     _lib = L
     return L
 
@@ -438,6 +453,92 @@ class Tissue:
     def get_order_parameter(self):
         phi, _ = self.sim.order_parameter()
         return phi[:, 0]
+
+
+@dataclass
+class RefParams:
+    """Parameters of the reference-semantics step: the _2DTissue ctor defaults (2DTissue.h:37-54)."""
+    v0: float = 0.1
+    k: float = 1.0
+    sigma: float = 0.41667
+    r_adh: float = 1.0
+    k_adh: float = 0.75
+    step_size: float = 0.001
+
+    def to_c(self):
+        return _RefParams(*[float(v) for v in asdict(self).values()])
+
+
+def ref_vertex_distances(mesh):
+    """Chart-vertex distance matrix (shortest paths along mesh edges), Vuv x Vuv."""
+    out = np.zeros((mesh.Vuv, mesh.Vuv))
+    rc = lib().tds_ref_vertex_distances(mesh.h, out.ctypes.data)
+    if rc != TDS_OK:
+        raise TdsError(rc, "vertex distances failed")
+    return out
+
+
+class RefSimulation:
+    """The reference's own step on the device (FP64): integer-degree polarity, vertex-snapped pair
+    distances from a dense matrix, chart-difference forces, brute-force face search
+    (tds_ref_* in include/tds.h)."""
+
+    def __init__(self, mesh, params, n_particles, seed=0, vertex_dist=None):
+        self.mesh = mesh
+        self.N = int(n_particles)
+        D = None if vertex_dist is None else np.ascontiguousarray(vertex_dist, np.float64)
+        if D is not None and D.shape != (mesh.Vuv, mesh.Vuv):
+            raise ValueError("vertex_dist must be Vuv x Vuv")
+        h = C.c_void_p()
+        p = params.to_c()
+        rc = lib().tds_ref_create(mesh.h, _ptr(D), C.byref(p), self.N, C.c_uint64(seed), C.byref(h))
+        if rc != TDS_OK:
+            raise TdsError(rc, "ref create failed (no CUDA device, bad parameters or size limit)")
+        self.h = h
+
+    def _check(self, rc):
+        if rc != TDS_OK:
+            raise TdsError(rc, lib().tds_ref_last_error(self.h).decode())
+
+    def start(self):
+        self._check(lib().tds_ref_start(self.h))
+
+    def set_state(self, r_uv, n_deg, nearest=None):
+        u = np.ascontiguousarray(r_uv, np.float64)
+        n = np.ascontiguousarray(n_deg, np.int32)
+        nv = None if nearest is None else np.ascontiguousarray(nearest, np.int32)
+        self._check(lib().tds_ref_set_state(self.h, u.ctypes.data, n.ctypes.data, _ptr(nv)))
+
+    def step(self, n=1):
+        self._check(lib().tds_ref_step(self.h, int(n)))
+
+    def get_state(self):
+        N = self.N
+        out = dict(uv=np.zeros((N, 2)), n_deg=np.zeros(N, np.int32), nearest=np.zeros(N, np.int32),
+                   r3d=np.zeros((N, 3)), r_dot=np.zeros((N, 2)), nbr=np.zeros(N, np.int32))
+        self._check(lib().tds_ref_get_state(self.h, *[out[k].ctypes.data for k in
+                                                      ("uv", "n_deg", "nearest", "r3d", "r_dot", "nbr")]))
+        return out
+
+    def order_parameter(self):
+        n = C.c_int()
+        self._check(lib().tds_ref_get_order_parameter(self.h, None, 0, C.byref(n)))
+        out = np.zeros(n.value)
+        self._check(lib().tds_ref_get_order_parameter(self.h, out.ctypes.data, n.value, C.byref(n)))
+        return out
+
+    def stream(self):
+        s = C.c_void_p()
+        self._check(lib().tds_ref_stream(self.h, C.byref(s)))
+        return s.value
+
+    def close(self):
+        if getattr(self, "h", None) is not None and _lib is not None:
+            _lib.tds_ref_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 def autotune(mesh, params, n_particles, seed=0, precision=32, trial_steps=64):

@@ -19,8 +19,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 
 HOST_SRCS = ["mesh.cpp", "geometry.cpp"]
-CUDA_SRCS = ["capi.cu"]
-HEADERS = ["mesh.hpp", "geometry.hpp", "kernels.cuh", "philox.cuh"]
+CUDA_SRCS = ["capi.cu", "ref_step.cu"]
+# ref_step.cu restates the reference's FP64 arithmetic: no multiply-add contraction, so that it
+# rounds like the oracle (built with -ffp-contract=off)
+CUDA_FLAGS = {"ref_step.cu": ["--fmad=false"]}
+HEADERS = ["mesh.hpp", "geometry.hpp", "kernels.cuh", "philox.cuh", "adjoint.cuh"]
 
 
 def _run(cmd):
@@ -54,7 +57,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
             cmd = [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda",
-                                   "-Xcompiler", "-fPIC,-ffp-contract=off", "-c", s, "-o", o]
+                                   "-Xcompiler", "-fPIC,-ffp-contract=off", "-c", s, "-o", o] + CUDA_FLAGS.get(src, [])
             if ptxas_info:
                 cmd += ["-Xptxas", "-v"]
             jobs.append(cmd)

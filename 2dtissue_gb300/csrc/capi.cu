@@ -99,14 +99,19 @@ struct tds_sim {
     int* packed_ids = nullptr;
     void* noise = nullptr;
     size_t noise_cap = 0;
-    double* st_d = nullptr;  // output staging (double) 8N
-    int* st_i = nullptr;     // output staging (int) 2N
-    double* in_d = nullptr;  // input staging (double) 6N
-    int* in_i = nullptr;     // input staging (int) N
+    // transfer staging, two of each so that a transfer of call k+1 can run while call k's
+    // buffer is still in use on the other side (the gather of step k+1 during the download of
+    // step k; the upload of step k+1 before the load of step k has run)
+    double* st_d[2] = {nullptr, nullptr};  // output staging (double) 8N
+    int* st_i[2] = {nullptr, nullptr};     // output staging (int) 2N
+    double* in_d[2] = {nullptr, nullptr};  // input staging (double) 6N
+    int* in_i[2] = {nullptr, nullptr};     // input staging (int) N
+    int in_next = 0, out_next = 0;         // staging buffer of the next upload / download
     // state transfers: uploads and downloads on their own streams, so that the two directions of
     // the host link run at the same time; events order them against the compute stream
     cudaStream_t up = nullptr, down = nullptr;
-    cudaEvent_t ev_in_ready = nullptr, ev_in_free = nullptr, ev_out_ready = nullptr, ev_out_free = nullptr;
+    cudaEvent_t ev_in_ready[2] = {nullptr, nullptr}, ev_in_free[2] = {nullptr, nullptr};
+    cudaEvent_t ev_out_ready[2] = {nullptr, nullptr}, ev_out_free[2] = {nullptr, nullptr};
     int cur = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int graph_steps = 16;        // steps per captured CUDA graph (tuning; even)
@@ -315,10 +320,12 @@ int alloc_state(tds_sim* s) {
     if ((rc = dalloc(s, &s->phi_pending, sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->d_step, sizeof(long long)))) return rc;
     if ((rc = dalloc(s, &s->packed_ids, N * sizeof(int)))) return rc;
-    if ((rc = dalloc(s, &s->st_d, 8 * N * sizeof(double)))) return rc;
-    if ((rc = dalloc(s, &s->st_i, 2 * N * sizeof(int)))) return rc;
-    if ((rc = dalloc(s, &s->in_d, 6 * N * sizeof(double)))) return rc;
-    if ((rc = dalloc(s, &s->in_i, N * sizeof(int)))) return rc;
+    for (int b = 0; b < 2; ++b) {
+        if ((rc = dalloc(s, &s->st_d[b], 8 * N * sizeof(double)))) return rc;
+        if ((rc = dalloc(s, &s->st_i[b], 2 * N * sizeof(int)))) return rc;
+        if ((rc = dalloc(s, &s->in_d[b], 6 * N * sizeof(double)))) return rc;
+        if ((rc = dalloc(s, &s->in_i[b], N * sizeof(int)))) return rc;
+    }
     CK(cudaMemset(s->count, 0, (size_t)s->M * sizeof(int)));
     CK(cudaMemset(s->tile_sum, 0, (size_t)2 * s->n_tiles * sizeof(int)));
     CK(cudaMemset(s->phi_acc, 0, (size_t)s->R * tdsk::kPhiCopies * 6 * sizeof(unsigned long long)));
@@ -593,21 +600,21 @@ struct Arena {
 // Loads the state waiting in the input staging (k_load_state computes polarity, cell keys and
 // counts) on the compute stream; per-tile counts for the next scan.
 template <typename real>
-int load_from_staging(tds_sim* s, bool has_face, bool has_r3d, bool sync) {
+int load_from_staging(tds_sim* s, int b, bool has_face, bool has_r3d, bool sync) {
     const size_t N = (size_t)s->N;
     s->cur = 0;
     const int nb = (s->N + 255) / 256;
     CK(cudaMemsetAsync(s->count, 0, (size_t)s->M * sizeof(int), s->stream));
     CK(cudaMemsetAsync(s->tile_sum, 0, (size_t)2 * s->n_tiles * sizeof(int), s->stream));
     tdsk::k_load_state<real><<<nb, 256, 0, s->stream>>>(
-        s->in_d, s->in_d + 2 * N, s->in_i, s->in_d + 3 * N, has_face, has_r3d, (const real*)s->rec, s->adj, s->G,
+        s->in_d[b], s->in_d[b] + 2 * N, s->in_i[b], s->in_d[b] + 3 * N, has_face, has_r3d, (const real*)s->rec, s->adj, s->G,
         s->bin_start, s->bin_faces, s->packed_ids, (const RepParams<real>*)s->reps, s->local_bits, s->rows, s->ivals,
         (R4<real>*)s->pos[0], (R4<real>*)s->pol[0], (R2<real>*)s->uv[0], s->ids[0], (R2<real>*)s->vel[0], s->cnt[0],
         s->key[0], s->count, s->N, s->status);
     tdsk::k_tile_sums<<<s->n_tiles, tdsk::kScanThreads, 0, s->stream>>>(s->count, s->M, s->tile_sum, s->n_tiles,
                                                                          s->d_step);
     CK(cudaGetLastError());
-    CK(cudaEventRecord(s->ev_in_free, s->stream));
+    CK(cudaEventRecord(s->ev_in_free[b], s->stream));
     if (sync) CK(cudaStreamSynchronize(s->stream));
     return TDS_OK;
 }
@@ -623,18 +630,20 @@ int load_state(tds_sim* s, const tds_state_view* in, bool sync) {
         for (size_t i = 0; i < N; ++i) fmax = std::max(fmax, in->face[i]);
         if (fmax >= s->mesh->t.F) return fail(s, TDS_ERR_ARG, "set_state: face index out of range");
     }
-    double* d_uv = s->in_d;
-    double* d_th = s->in_d + 2 * N;
-    double* d_r3 = s->in_d + 3 * N;
-    int* d_face = s->in_i;
-    CK(cudaStreamWaitEvent(s->up, s->ev_in_free, 0));
+    const int b = s->in_next;
+    s->in_next ^= 1;
+    double* d_uv = s->in_d[b];
+    double* d_th = s->in_d[b] + 2 * N;
+    double* d_r3 = s->in_d[b] + 3 * N;
+    int* d_face = s->in_i[b];
+    CK(cudaStreamWaitEvent(s->up, s->ev_in_free[b], 0));
     CK(cudaMemcpyAsync(d_uv, in->uv, 2 * N * sizeof(double), cudaMemcpyHostToDevice, s->up));
     CK(cudaMemcpyAsync(d_th, in->theta, N * sizeof(double), cudaMemcpyHostToDevice, s->up));
     if (in->face) CK(cudaMemcpyAsync(d_face, in->face, N * sizeof(int), cudaMemcpyHostToDevice, s->up));
     if (in->r3d) CK(cudaMemcpyAsync(d_r3, in->r3d, 3 * N * sizeof(double), cudaMemcpyHostToDevice, s->up));
-    CK(cudaEventRecord(s->ev_in_ready, s->up));
-    CK(cudaStreamWaitEvent(s->stream, s->ev_in_ready, 0));
-    return load_from_staging<real>(s, in->face != nullptr, in->r3d != nullptr, sync);
+    CK(cudaEventRecord(s->ev_in_ready[b], s->up));
+    CK(cudaStreamWaitEvent(s->stream, s->ev_in_ready[b], 0));
+    return load_from_staging<real>(s, b, in->face != nullptr, in->r3d != nullptr, sync);
 }
 
 // Places particles on the device (k_place) into the input staging and loads them.
@@ -664,11 +673,14 @@ int start_device(tds_sim* s) {
     CK(cudaMemcpy(dpr, pr.data(), pr.size() * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(dcdf, t.area_cdf.data(), (size_t)F * sizeof(double), cudaMemcpyHostToDevice));
     const size_t N = (size_t)s->N;
-    CK(cudaStreamWaitEvent(s->stream, s->ev_in_free, 0));
+    const int b = s->in_next;
+    s->in_next ^= 1;
+    CK(cudaStreamWaitEvent(s->stream, s->ev_in_free[b], 0));
     tdsk::k_place<<<(s->N + 255) / 256, 256, 0, s->stream>>>(dpr, dcdf, F, s->packed_ids, s->local_bits, s->seed,
-                                                              s->in_d, s->in_d + 2 * N, s->in_i, s->in_d + 3 * N, s->N);
+                                                              s->in_d[b], s->in_d[b] + 2 * N, s->in_i[b],
+                                                              s->in_d[b] + 3 * N, s->N);
     CK(cudaGetLastError());
-    return load_from_staging<real>(s, true, true, true);  // synchronises before the tables are freed
+    return load_from_staging<real>(s, b, true, true, true);  // synchronises before the tables are freed
 }
 
 // Output: gather into the output staging on the compute stream, then device -> host on the
@@ -676,22 +688,24 @@ int start_device(tds_sim* s) {
 template <typename real>
 int save_state(tds_sim* s, tds_state_view* out, bool sync) {
     const size_t N = (size_t)s->N;
-    double* d_uv = s->st_d;
-    double* d_th = s->st_d + 2 * N;
-    double* d_r3 = s->st_d + 3 * N;
-    double* d_vel = s->st_d + 6 * N;
-    int* d_face = s->st_i;
-    int* d_cnt = s->st_i + N;
+    const int b = s->out_next;
+    s->out_next ^= 1;
+    double* d_uv = s->st_d[b];
+    double* d_th = s->st_d[b] + 2 * N;
+    double* d_r3 = s->st_d[b] + 3 * N;
+    double* d_vel = s->st_d[b] + 6 * N;
+    int* d_face = s->st_i[b];
+    int* d_cnt = s->st_i[b] + N;
     const int c = s->cur;
     const int nb = (s->N + 255) / 256;
-    CK(cudaStreamWaitEvent(s->stream, s->ev_out_free, 0));
+    CK(cudaStreamWaitEvent(s->stream, s->ev_out_free[b], 0));
     tdsk::k_gather_state<real><<<nb, 256, 0, s->stream>>>(
         (const R4<real>*)s->pos[c], (const R4<real>*)s->pol[c], (const R2<real>*)s->uv[c], s->ids[c],
         (const R2<real>*)s->vel[c], s->cnt[c], (const RepParams<real>*)s->reps, s->local_bits, d_uv, d_th, d_face, d_r3,
         d_vel, d_cnt, s->N);
     CK(cudaGetLastError());
-    CK(cudaEventRecord(s->ev_out_ready, s->stream));
-    CK(cudaStreamWaitEvent(s->down, s->ev_out_ready, 0));
+    CK(cudaEventRecord(s->ev_out_ready[b], s->stream));
+    CK(cudaStreamWaitEvent(s->down, s->ev_out_ready[b], 0));
     cudaStream_t d = s->down;
     if (out->uv) CK(cudaMemcpyAsync(out->uv, d_uv, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, d));
     if (out->theta) CK(cudaMemcpyAsync(out->theta, d_th, N * sizeof(double), cudaMemcpyDeviceToHost, d));
@@ -699,7 +713,7 @@ int save_state(tds_sim* s, tds_state_view* out, bool sync) {
     if (out->r3d) CK(cudaMemcpyAsync(out->r3d, d_r3, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, d));
     if (out->vel_uv) CK(cudaMemcpyAsync(out->vel_uv, d_vel, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, d));
     if (out->nbr_count) CK(cudaMemcpyAsync(out->nbr_count, d_cnt, N * sizeof(int), cudaMemcpyDeviceToHost, d));
-    CK(cudaEventRecord(s->ev_out_free, d));
+    CK(cudaEventRecord(s->ev_out_free[b], d));
     if (sync) CK(cudaStreamSynchronize(d));
     return TDS_OK;
 }
@@ -1094,7 +1108,8 @@ int create_impl(const tds_mesh* mesh, int R, const int* n, const tds_params* prm
         tds_destroy(s.release());
         return TDS_ERR_CUDA;
     }
-    for (cudaEvent_t* e : {&s->ev_in_ready, &s->ev_in_free, &s->ev_out_ready, &s->ev_out_free})
+    for (cudaEvent_t* e : {&s->ev_in_ready[0], &s->ev_in_free[0], &s->ev_out_ready[0], &s->ev_out_free[0],
+                           &s->ev_in_ready[1], &s->ev_in_free[1], &s->ev_out_ready[1], &s->ev_out_free[1]})
         if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) {
             tds_destroy(s.release());
             return TDS_ERR_CUDA;
@@ -1416,7 +1431,8 @@ void tds_destroy(tds_sim* s) {
     for (void* p : s->allocs) cudaFree(p);
     if (s->series) cudaFree(s->series);
     if (s->noise) cudaFree(s->noise);
-    for (cudaEvent_t e : {s->ev_in_ready, s->ev_in_free, s->ev_out_ready, s->ev_out_free})
+    for (cudaEvent_t e : {s->ev_in_ready[0], s->ev_in_free[0], s->ev_out_ready[0], s->ev_out_free[0],
+                          s->ev_in_ready[1], s->ev_in_free[1], s->ev_out_ready[1], s->ev_out_free[1]})
         if (e) cudaEventDestroy(e);
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->up) cudaStreamDestroy(s->up);

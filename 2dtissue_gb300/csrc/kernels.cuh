@@ -755,10 +755,23 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(int* __restrict__ count, 
         finalize_replica(fin, (int)blockIdx.x - n_tiles, *d_step, s_fin);
         return;
     }
-    const int par = (int)((*d_step + 1) & 1);
-    const int* ts = tile_sum + (size_t)par * n_tiles;
     const int tile = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // this thread's counts, loaded first so that their latency overlaps the block-base sum
+    const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
+    int v[kScanItems];
+    if (base + kScanItems <= M) {
+#pragma unroll
+        for (int i = 0; i < kScanItems; i += 4) {
+            const int4 x = *reinterpret_cast<const int4*>(count + base + i);
+            v[i] = x.x, v[i + 1] = x.y, v[i + 2] = x.z, v[i + 3] = x.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < kScanItems; ++i) v[i] = base + i < M ? count[base + i] : 0;
+    }
+    const int par = (int)((*d_step + 1) & 1);
+    const int* ts = tile_sum + (size_t)par * n_tiles;
     // base = sum of ts[0..tile)
     int part = 0;
     for (int i = threadIdx.x; i < tile; i += kScanThreads) part += ts[i];
@@ -773,19 +786,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(int* __restrict__ count, 
         tile_sum[(size_t)(par ^ 1) * n_tiles + tile] = 0;
     }
     __syncthreads();
-    const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
-    int v[kScanItems];
     int sum = 0;
-    if (base + kScanItems <= M) {
-#pragma unroll
-        for (int i = 0; i < kScanItems; i += 4) {
-            const int4 x = *reinterpret_cast<const int4*>(count + base + i);
-            v[i] = x.x, v[i + 1] = x.y, v[i + 2] = x.z, v[i + 3] = x.w;
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < kScanItems; ++i) v[i] = base + i < M ? count[base + i] : 0;
-    }
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) sum += v[i];
     int incl = sum;

@@ -70,13 +70,44 @@ def profiled_traffic(n_particles):
     return None
 
 
+class _Nvml:
+    """Read-only NVML queries through ctypes (SM clock, max SM clock, clock-event reasons)."""
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, index):
+        import ctypes as C
+        self.C = C
+        self.lib = C.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = C.c_void_p()
+        if self.lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(index), C.byref(self.h)) != 0:
+            raise OSError("no NVML device %d" % index)
+        reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
+        self.reasons_fn = reasons_fn or self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def sample(self):
+        C = self.C
+        mhz, r = C.c_uint(0), C.c_ulonglong(0)
+        ok = self.lib.nvmlDeviceGetClockInfo(self.h, C.c_int(1), C.byref(mhz)) == 0  # NVML_CLOCK_SM
+        self.reasons_fn(self.h, C.byref(r))
+        return (float(mhz.value) if ok else None), int(r.value)
+
+    def max_sm(self):
+        C = self.C
+        mhz = C.c_uint(0)
+        return float(mhz.value) if self.lib.nvmlDeviceGetMaxClockInfo(self.h, C.c_int(1), C.byref(mhz)) == 0 else None
+
+
 class Clocks:
-    """nvidia-smi samples during the timed region."""
+    """SM clocks and clock-event reasons during the timed region: an NVML poller every 5 ms (the
+    timed region can be shorter than nvidia-smi's sampling period) and nvidia-smi at 200 ms."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
+        import threading
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), "--query-gpu=" + self.Q,
@@ -84,14 +115,32 @@ class Clocks:
                                       stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
+        self.nv_samples, self.nv_max = [], None
+        self.done = threading.Event()
+        self.t = None
+        try:
+            self.nv = _Nvml(index)
+            self.nv_max = self.nv.max_sm()
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+        except (OSError, AttributeError):
+            self.nv = None
+
+    def _poll(self):
+        while not self.done.is_set():
+            self.nv_samples.append(self.nv.sample())
+            self.done.wait(0.005)
 
     def stop(self):
-        if self.p is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.p.terminate()
-        self.p.wait()
-        self.f.seek(0)
-        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        self.done.set()
+        if self.t is not None:
+            self.t.join()
+        rows = []
+        if self.p is not None:
+            self.p.terminate()
+            self.p.wait()
+            self.f.seek(0)
+            rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
         os.unlink(self.f.name)
         sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
         mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
@@ -103,8 +152,19 @@ class Clocks:
             for k, nm in enumerate(names):
                 if r[5 + k].strip().lower() == "active":
                     reasons.add(nm)
+        nv_sm = [s for s, _ in self.nv_samples if s is not None]
+        for _, bits in self.nv_samples:
+            for b, nm in _Nvml.REASONS.items():
+                if bits & b:
+                    reasons.add(nm)
+        if nv_sm:
+            return {"sm_mhz": float(np.median(nv_sm)), "sm_max_mhz": self.nv_max or (max(mx) if mx else None),
+                    "reasons": sorted(reasons), "samples": len(nv_sm), "source": "NVML every 5 ms",
+                    "nvidia_smi_samples": len(rows)}
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(rows)}
+                "reasons": sorted(reasons), "samples": len(rows), "source": "nvidia-smi every 200 ms"}
 
 
 def dist_setup(args):
@@ -189,8 +249,8 @@ def run_reference(args):
         out = oracle.model_step(om, p.oracle_dict(), st, k, 0, centroid=cen, threads=cores)
         st = dict(uv=out["uv"], theta=out["theta"], face=out["face"], r3d=out["r3d"], ids=st["ids"])
     t_full = (time.perf_counter() - t0) / max(args.warmup, 1)
-    # bounded sample: update a subset when the full K steps would exceed ~150 s
-    m = n if args.steps * t_full <= 150 else max(4096, int(n * 150 / (args.steps * t_full)))
+    # bounded sample: update a subset when the full K steps would exceed ~60 s
+    m = n if args.steps * t_full <= 60 else max(4096, int(n * 60 / (args.steps * t_full)))
     sub = None if m == n else np.sort(np.random.default_rng(1).choice(n, m, replace=False)).astype(np.int32)
     t0 = time.perf_counter()
     for k in range(args.steps):
@@ -228,35 +288,37 @@ def run_gpu(args):
             flush.fill_(k & 255)
 
     for k in range(args.warmup):
-        flush_l2(k)
-        sim.step_async(1)
+        sim.step_async(16)
     torch.cuda.synchronize()
     assert sim.status() == 0, "device status set during warm-up"
 
-    # ---- timed region: K steps, each flushed + event-timed ----
-    sim.kernel_timing(True)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    # ---- timed region: K steps back to back, launched as the library launches them (CUDA graphs
+    # of 16 steps); the per-step working set (state, its sorted copy, cell tables, cell
+    # descriptors, face records: ~220 MB) is larger than the 126 MB L2, so no flush ----
+    ga, gb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(world)
     torch.cuda.synchronize()
     clk = Clocks(local)
-    for k in range(args.steps):
-        flush_l2(k + 7)
-        ev[k][0].record(stream)
-        sim.step_async(1)
-        ev[k][1].record(stream)
+    ga.record(stream)
+    sim.step_async(args.steps)
+    gb.record(stream)
     torch.cuda.synchronize()
     barrier(world)
     clocks = clk.stop()
-    total_ms = sum(a.elapsed_time(b) for a, b in ev)
-    kt = sim.kernel_times()
-    sim.kernel_timing(False)
+    total_ms = ga.elapsed_time(gb)
     status = sim.status()
     if status:
         raise SystemExit("device status 0x%x in the timed region" % status)
     total_ms = allreduce_max(total_ms, world)
     value = world * n * args.steps / (total_ms * 1e-3)
 
-    # ---- dominant kernel roofline (k_step), from the events of the timed region ----
+    # ---- per-kernel events over the same K steps launched one by one (no graphs): the dominant
+    # kernel's duration for the roofline, and each kernel's share of the step ----
+    sim.kernel_timing(True)
+    sim.step_async(args.steps)
+    torch.cuda.synchronize()
+    kt = sim.kernel_times()
+    sim.kernel_timing(False)
     step_ms, step_n = kt["step"]
     avg_s = step_ms * 1e-3 / max(step_n, 1)
     alg = ALG_BYTES_PARTICLE * n + ALG_BYTES_FACE * mesh.F + ALG_BYTES_REPLICA
@@ -269,15 +331,17 @@ def run_gpu(args):
     step_frac = alg / (total_ms * 1e-3 / args.steps) / 1e9 / peak
     shares = {k: v[0] / max(1e-12, sum(x[0] for x in kt.values())) for k, v in kt.items()}
 
-    # ---- steady state: graph-captured back-to-back steps, no flush (informational) ----
-    ga, gb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    sim.step_async(16)
+    # ---- each step after a 256 MB L2 flush, event-timed per step (informational) ----
+    fl_steps = min(args.steps, 50)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(fl_steps)]
+    for k in range(fl_steps):
+        flush_l2(k + 7)
+        ev[k][0].record(stream)
+        sim.step_async(1)
+        ev[k][1].record(stream)
     torch.cuda.synchronize()
-    ga.record(stream)
-    sim.step_async(128)
-    gb.record(stream)
-    torch.cuda.synchronize()
-    loop_rate = n * 128 / (ga.elapsed_time(gb) * 1e-3)
+    flushed_ms = allreduce_max(sum(a.elapsed_time(b) for a, b in ev), world)
+    flushed_rate = world * n * fl_steps / (flushed_ms * 1e-3)
 
     # ---- end to end through the C-ABI with pinned host buffers ----
     def pinned(shape, dtype):
@@ -336,9 +400,11 @@ def run_gpu(args):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded placement)",
-                "config": workload_config(mesh, p, n, "flushed (256 MB write) before every timed step"),
+                "config": workload_config(mesh, p, n, "inputs larger than L2: ~220 MB touched per step vs 126 MB L2; "
+                                                      "steps back to back (CUDA graphs of 16 steps), no flush"),
                 "roofline": roofline, "step_hbm_frac": step_frac, "kernel_share": shares,
-                "graph_loop": {"value": loop_rate, "unit": UNIT, "note": "128 graph-captured steps, no flush"},
+                "flushed_per_step": {"value": flushed_rate, "unit": UNIT, "steps": fl_steps,
+                                     "note": "each step after a 256 MB L2 flush, event-timed per step"},
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": sim.kernels_per_step() * args.steps, "clocks": clocks,
                 "parallelism": "replicas only (one independent 1M-particle system per GPU)"}
         print(json.dumps(line), flush=True)
@@ -416,7 +482,7 @@ def run_adjoint(args):
     tg = importlib.import_module("2dtissue_gb300")
     mesh = tg.Mesh.ellipsoid(4, (6.0, 3.0, 3.0))
     n = 10000
-    T = args.steps if args.steps != 50 else 2000
+    T = args.steps
     target = tg.Params(v0=1.0, k_rep=10.0, tau=1.0, align=0.5)
     pert = tg.Params(v0=1.1, k_rep=9.0, tau=1.2, align=0.4)
     ref = tg.Simulation(mesh, target, n, seed=0, precision=32)
@@ -468,7 +534,7 @@ def run_adjoint_batched(args):
     mesh = tg.Mesh.bumpy_sphere(6, 0.2, 5.0)
     rng = np.random.default_rng(5)
     R = 512
-    T = args.steps if args.steps != 50 else 500
+    T = args.steps
     ns = [int(x) for x in rng.integers(1000, 20001, size=R)]
     ps = [tg.Params(v0=float(rng.uniform(0.5, 1.5)), k_rep=float(rng.uniform(5, 20)), tau=float(rng.uniform(0.5, 2)),
                     eta=float(rng.uniform(0.1, 1.0))) for _ in range(R)]
@@ -506,6 +572,57 @@ def run_adjoint_batched(args):
     print(json.dumps(line), flush=True)
 
 
+def run_ref(args):
+    """Reference-semantics step (tds_ref_*: the reference's own algorithm, FP64) on the (2,1,1)
+    ellipsoid (level-4 icosphere): 100 particles with the 100-particle system's values (R 0.05,
+    k 10, v0 1, dt 0.02) and 2,000 particles with the reference's constructor defaults, `steps`
+    steps each (default 50), against the oracle's ref-form step on one host core (the reference is
+    single-threaded) over a bounded sample of steps."""
+    import torch
+    tg = importlib.import_module("2dtissue_gb300")
+    import oracle
+    mesh = tg.Mesh.ellipsoid(4, (2.0, 1.0, 1.0))
+    a = mesh.arrays()
+    D = tg.ref_vertex_distances(mesh)
+    T = args.steps
+    cases = [("100 particles, R 0.05, k 10, v0 1, dt 0.02", 100,
+              dict(v0=1.0, k=10.0, sigma=0.05, r_adh=0.12, k_adh=0.75, step_size=0.02)),
+             ("2,000 particles, reference ctor defaults", 2000,
+              dict(v0=0.1, k=1.0, sigma=0.41667, r_adh=1.0, k_adh=0.75, step_size=0.001))]
+    out = []
+    for name, n, prm in cases:
+        sim = tg.RefSimulation(mesh, tg.RefParams(**prm), n, seed=0, vertex_dist=D)
+        sim.start()
+        sim.step(max(args.warmup, 3))
+        s0 = sim.get_state()
+        stream = torch.cuda.ExternalStream(sim.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sim.step(T)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        gpu_rate = n * T / (e0.elapsed_time(e1) * 1e-3)
+        sim.close()
+        st = dict(uv=s0["uv"], n_deg=s0["n_deg"], nearest=s0["nearest"])
+        k, t0 = 0, time.perf_counter()
+        while k < T and time.perf_counter() - t0 < 15.0:
+            o = oracle.ref_step(a, D, prm, st["uv"], st["n_deg"], st["nearest"])
+            st = dict(uv=o["uv"], n_deg=o["n_deg"], nearest=o["nearest"])
+            k += 1
+        cpu_rate = n * k / (time.perf_counter() - t0)
+        out.append({"case": name, "particles": n, "steps": T, "value": gpu_rate, "unit": UNIT,
+                    "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": 1, "kind": "port",
+                                     "sample": "%d steps of the ref-form oracle step (orc_ref_step)" % k},
+                    "gpu_over_cpu": gpu_rate / cpu_rate})
+    line = {"metric": "particle-steps/s (reference-semantics step, FP64)", "value": out[0]["value"], "unit": UNIT,
+            "n_gpus": 1, "steps": T, "warmup": args.warmup, "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic (seeded centroid placement)",
+            "config": {"workload": "reference-semantics step, (2,1,1) ellipsoid L4 (Vuv %d, F %d)" % (mesh.Vuv, mesh.F)},
+            "cases": out}
+    print(json.dumps(line), flush=True)
+
+
 def run_profile(args):
     """Minimal driver for ncu: the 1M-particle system, `warmup` steps, then `steps` steps; no timing."""
     import torch
@@ -523,16 +640,19 @@ def run_profile(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: plain 500, ensemble 50, adjoint 2000, adjoint_batched 500, ref 50)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", action="store_true", help="only run warmup + steps (for ncu)")
-    ap.add_argument("--workload", default="plain", choices=["plain", "ensemble", "adjoint", "adjoint_batched"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "ensemble", "adjoint", "adjoint_batched", "ref"])
     ap.add_argument("--replicas", type=int, default=4096, help="ensemble workload: replicas")
     ap.add_argument("--sample", type=int, default=256, help="ensemble workload: replicas run one by one")
     ap.add_argument("--autotune", action="store_true", help="ensemble workload: time the autotuner's choice")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = {"plain": 500, "ensemble": 50, "adjoint": 2000, "adjoint_batched": 500, "ref": 50}[args.workload]
     if args.profile:
         return run_profile(args)
     if args.workload == "ensemble" and args.impl != "reference":
@@ -541,6 +661,8 @@ def main():
         return run_adjoint(args)
     if args.workload == "adjoint_batched" and args.impl != "reference":
         return run_adjoint_batched(args)
+    if args.workload == "ref" and args.impl != "reference":
+        return run_ref(args)
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":

@@ -199,6 +199,53 @@ int tds_kernels_per_step(const tds_sim* sim, int* n);
 const char* tds_last_error(const tds_sim* sim);
 void tds_destroy(tds_sim* sim);
 
+/* ---- reference-semantics step (FP64, small meshes) ----
+ * The reference's own per-step algorithm on the device, for exact reference-semantics studies
+ * (the model-form calls above are the fast path). It keeps the reference's state and rules:
+ * integer-degree polarity n, the pair distance between the particles' nearest chart vertices read
+ * from a dense Vuv x Vuv matrix (Locomotion.cpp:94-138), chart-difference force directions with
+ * only |F| used (Locomotion.cpp:57-89, ForceHelper.cpp:34-104), the circular mean of the angles
+ * within 2 sigma truncated to int (OrientationHelper.cpp:29-116), the list-order seam wrap
+ * (EuclideanTiling.cpp:31-208), the brute-force chart face search with distance weights and the
+ * nearest corner (CellHelper.cpp:71-160), the neighbour count d != 0 && d <= 2.4 sigma
+ * (2DTissue.cpp:254-268) and, per step, |sum sign(u v' - v u')| / N as the order parameter (the
+ * reference's own evaluation reads out of bounds, LinearAlgebra.cpp:67-105). Cost is O(N^2 + N F)
+ * per step, as in the reference: N <= 65,536, Vuv <= 32,768. */
+typedef struct tds_ref_params { /* _2DTissue ctor arguments (2DTissue.h:37-54) */
+    double v0;        /* default 0.1 */
+    double k;         /* default 1 */
+    double sigma;     /* default 0.41667 */
+    double r_adh;     /* default 1 */
+    double k_adh;     /* default 0.75 */
+    double step_size; /* default 0.001 */
+} tds_ref_params;
+typedef struct tds_ref_sim tds_ref_sim;
+/* Shortest paths along the chart mesh's edges (3D edge lengths), Vuv x Vuv row-major into out:
+ * the stand-in for CachedGeodesicDistanceHelper::get_mesh_distance_matrix (2DTissue.cpp:102-105),
+ * whose library is absent. Paths do not cross the seam (the reference measures on the open mesh). */
+int tds_ref_vertex_distances(const tds_mesh* mesh, double* out);
+/* _2DTissue ctor (2DTissue.cpp:20-111): vertex_dist = Vuv x Vuv matrix, or NULL to compute
+ * tds_ref_vertex_distances. */
+int tds_ref_create(const tds_mesh* mesh, const double* vertex_dist, const tds_ref_params* params, int n_particles,
+                   uint64_t seed, tds_ref_sim** out);
+/* start() (2DTissue.cpp:117-134): init_particle_position (uniform face index, its chart centroid,
+ * uniform integer angle; Philox-seeded) and get_r3d. */
+int tds_ref_start(tds_ref_sim* sim);
+/* State in particle order: r_uv 2N, n_deg N; nearest_vertex N chart vertex ids or NULL (then
+ * taken from the face search, as get_r3d does). */
+int tds_ref_set_state(tds_ref_sim* sim, const double* r_uv, const int* n_deg, const int* nearest_vertex);
+/* update() physics (2DTissue.cpp:136-165, 222-252) n_steps times; TDS_ERR_STATE on a non-finite
+ * position (Validation::error_invalid_values) or a seam wrap that does not end. */
+int tds_ref_step(tds_ref_sim* sim, int n_steps);
+/* Any pointer may be NULL: r_uv 2N, n_deg N, nearest_vertex N, r3d 3N, r_dot 2N, nbr_count N. */
+int tds_ref_get_state(tds_ref_sim* sim, double* r_uv, int* n_deg, int* nearest_vertex, double* r3d, double* r_dot,
+                      int* nbr_count);
+/* get_order_parameter() (2DTissue.cpp:213-216): one value per step taken. */
+int tds_ref_get_order_parameter(tds_ref_sim* sim, double* out, int cap, int* n_steps);
+int tds_ref_stream(tds_ref_sim* sim, void** stream);
+const char* tds_ref_last_error(const tds_ref_sim* sim);
+void tds_ref_destroy(tds_ref_sim* sim);
+
 /* ---- test hooks ---- */
 /* Runs the device seam wrap (the model form of EuclideanTiling::diagonal_seam_edges_square_border,
  * EuclideanTiling.cpp:31-69) on n points: uv holds the advanced points on entry and the wrapped

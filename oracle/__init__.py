@@ -110,6 +110,29 @@ def ref_seam_wrap(uv_old, uv, n_deg):
     return u, n, uo
 
 
+def ref_step(arrays, dist_vv, params, r_uv, n_deg, nearest):
+    """One ref-form step (orc_ref_step) from (r_uv, n_deg, nearest); params holds the _2DTissue
+    ctor values v0, k, sigma, r_adh, k_adh, step_size. Returns the new state and the step's order
+    parameter."""
+    v3 = np.ascontiguousarray(arrays["v3"], np.float64)
+    f3 = np.ascontiguousarray(arrays["f3"], np.int32)
+    uv = np.ascontiguousarray(arrays["uv"], np.float64)
+    fuv = np.ascontiguousarray(arrays["fuv"], np.int32)
+    uv2v = np.ascontiguousarray(arrays["uv2v"], np.int32)
+    D = np.ascontiguousarray(dist_vv, np.float64)
+    u = np.array(r_uv, np.float64, order="C")
+    n = np.array(n_deg, np.int32)
+    near = np.array(nearest, np.int32)
+    N = len(n)
+    r3d, rdot, nbr, order = np.zeros((N, 3)), np.zeros((N, 2)), np.zeros(N, np.int32), np.zeros(1)
+    rc = lib().orc_ref_step(len(v3), v3, len(f3), f3, len(uv), uv, fuv, uv2v, D, params["v0"], params["k"],
+                            params["sigma"], params["r_adh"], params["k_adh"], params["step_size"], N, u, n, near,
+                            r3d, rdot, nbr, order)
+    if rc != 0:
+        raise RuntimeError("orc_ref_step failed (%d)" % rc)
+    return dict(uv=u, n_deg=n, nearest=near, r3d=r3d, r_dot=rdot, nbr=nbr, order=float(order[0]))
+
+
 def model_wrap(s_uv, e_uv, theta, vuv, max_wraps=8):
     s = np.array(s_uv, np.float64)
     e = np.array(e_uv, np.float64)
