@@ -115,7 +115,7 @@ struct tds_sim {
     int cur = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int graph_steps = 16;        // steps per captured CUDA graph (tuning; even)
-    int step_block = 256;        // threads per k_step block (tuning: 128 or 256)
+    int step_block = 128;        // threads per k_step block (tuning: 128 or 256)
     double cells_per_particle = 4.0;  // cell-level rule (tuning): finest level with C <= max(64, this * N_r)
     double origin[3] = {0, 0, 0};
     std::vector<void*> allocs;

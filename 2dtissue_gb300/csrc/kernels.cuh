@@ -228,14 +228,15 @@ __device__ __forceinline__ void face_frame(const real* g, real n[3], real Jp[6])
     Jp[3] = a12 * ux + a22 * vx, Jp[4] = a12 * uy + a22 * vy, Jp[5] = a12 * uz + a22 * vz;
 }
 
-// chart point -> 3D on face record h
+// chart point -> 3D on face record h (multiply-adds written out: the step and the state load
+// produce the same bits for the same chart point)
 template <typename real>
 __device__ __forceinline__ void face_map(const real* h, real u, real v, real& x, real& y, real& z) {
     const R4<real> q0 = rq(h, 0), q1 = rq(h, 1), q2 = rq(h, 2), q3 = rq(h, 3);
     const real du = u - q0.x, dv = v - q0.y;
-    x = q1.w + q2.x * du + q2.w * dv;
-    y = q3.z + q2.y * du + q3.x * dv;
-    z = q3.w + q2.z * du + q3.y * dv;
+    x = d_fma(q2.w, dv, d_fma(q2.x, du, q1.w));
+    y = d_fma(q3.x, dv, d_fma(q2.y, du, q3.z));
+    z = d_fma(q3.y, dv, d_fma(q2.z, du, q3.w));
 }
 template <typename real>
 __device__ __forceinline__ int bin_coord(real x, int G) {
@@ -422,18 +423,21 @@ template <typename real>
 __device__ __forceinline__ void pair_term(const PairC<real>& rp, const R4<real>& P, const R4<real>& Q,
                                           const R4<real>* __restrict__ pol, int j, bool self, real (&acc)[6],
                                           int& cnt) {
+    // every multiply-add is written out (d_fma / d_mul), so that each inlined copy of this
+    // function (the step kernel's single-system and ensemble loops, the adjoint's recompute)
+    // rounds identically whatever the compiler would contract
     const real dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
-    const real d2 = dx * dx + dy * dy + dz * dz;
+    const real d2 = d_fma(dz, dz, d_fma(dy, dy, d_mul(dx, dx)));
     if (d2 < rp.r_max2 && !self) {
         const R4<real> QL = pol[j];  // polarity only for neighbours (about a third of candidates)
         const real rd = d_rsqrt(d2);  // 1/d (d2 > 0 unless two particles coincide)
-        const real d = d2 * rd;
-        const real fm = d < rp.twoR ? rp.k * (rp.twoR - d) * rp.inv_twoR : -(rp.adh_scale * (d - rp.twoR));
+        const real d = d_mul(d2, rd);
+        const real fm = d < rp.twoR ? d_mul(d_mul(rp.k, rp.twoR - d), rp.inv_twoR) : -d_mul(rp.adh_scale, d - rp.twoR);
         if (d2 > (real)0) {
-            const real c = fm * rd;
-            acc[0] += c * dx;
-            acc[1] += c * dy;
-            acc[2] += c * dz;
+            const real c = d_mul(fm, rd);
+            acc[0] = d_fma(c, dx, acc[0]);
+            acc[1] = d_fma(c, dy, acc[1]);
+            acc[2] = d_fma(c, dz, acc[2]);
         }
         acc[3] += QL.x;
         acc[4] += QL.y;
@@ -449,15 +453,19 @@ __device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<re
 }
 
 // Pair sums over a particle's candidate runs in a fixed order (runs 0..8, slots ascending), two
-// candidates per iteration.
-template <typename real>
-__device__ __forceinline__ void pair_sums(const PairC<real>& pc, const R4<real>& P, const R4<real>* __restrict__ pos,
-                                          const R4<real>* __restrict__ pol, const int2 (&run)[9], int total, int self,
+// candidates per iteration. The run table lives in shared memory, one column per thread (entry r of
+// thread t at srun[r * BLOCK]): switching runs is a shared-memory load instead of a local-memory
+// (L1-cached stack) one, which took the step kernel from 142.7 to 137.0 us at 1M particles.
+template <typename real, int BLOCK>
+__device__ __forceinline__ void pair_sums_s(const PairC<real>& pc, const R4<real>& P, const R4<real>* __restrict__ pos,
+                                          const R4<real>* __restrict__ pol, const int2* srun, int total, int self,
                                           real (&acc)[6], int& cnt) {
-    int r = 0, t = run[0].x, left = run[0].y;
+    int r = 0;
+    int2 x0 = srun[0];
+    int t = x0.x, left = x0.y;
     for (int k = 0; k < total; k += 2) {
         while (left == 0) {
-            const int2 x = run[++r];
+            const int2 x = srun[(++r) * BLOCK];
             t = x.x;
             left = x.y;
         }
@@ -466,7 +474,7 @@ __device__ __forceinline__ void pair_sums(const PairC<real>& pc, const R4<real>&
         int tb = -1;
         if (k + 1 < total) {
             while (left == 0) {
-                const int2 x = run[++r];
+                const int2 x = srun[(++r) * BLOCK];
                 t = x.x;
                 left = x.y;
             }
@@ -481,9 +489,10 @@ __device__ __forceinline__ void pair_sums(const PairC<real>& pc, const R4<real>&
 }
 
 // BLOCK: threads per block (a tuning choice: 128 or 256); the register budget is the same either
-// way (5 blocks of 256, 10 of 128 per SM in FP32).
+// way (6 blocks of 256, 12 of 128 per SM in FP32: 40 registers; 6 rather than 5 blocks of 256 took the
+// step from 170.9 to 168.6 us at 1M particles).
 template <typename real, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 5 : 3) * 256 / BLOCK) k_step(const StepArgs<real> a) {
+__global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLOCK) k_step(const StepArgs<real> a) {
     typedef R4<real> r4;
     const int q = blockIdx.x * BLOCK + threadIdx.x;
     const bool active = q < a.N;
@@ -506,7 +515,8 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 5 : 3) * 256 / BLO
 
         // candidate ranges: the 9 x-runs of the particle's cell (static descriptors), as
         // (first slot, count) pairs so that the loop switches runs with one 8-byte load
-        int2 run[9];
+        __shared__ int2 s_run[9 * BLOCK];
+        int2* srun = s_run + threadIdx.x;
         int total = 0;
         const int id0 = key0 - rp.base;
         if (id0 < rp.C) {
@@ -519,12 +529,12 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 5 : 3) * 256 / BLO
                 const int b0 = rp.base + first;
                 const int t0 = len ? a.start[b0] : 0;
                 const int t1 = len ? a.start[b0 + len] : 0;
-                run[r] = make_int2(t0, t1 - t0);
+                srun[r * BLOCK] = make_int2(t0, t1 - t0);
                 total += t1 - t0;
             }
         } else {
 #pragma unroll
-            for (int r = 0; r < 9; ++r) run[r] = make_int2(0, 0);
+            for (int r = 0; r < 9; ++r) srun[r * BLOCK] = make_int2(0, 0);
         }
         // pair sums over all candidates (in a fixed order); a single-replica system takes the
         // pair constants from the kernel parameters (constant bank) rather than from the replica
@@ -532,9 +542,9 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 5 : 3) * 256 / BLO
         real acc[6] = {0, 0, 0, 0, 0, 0};
         int cnt = 0;
         if (a.single)
-            pair_sums(a.pc0, P, a.pos, a.pol, run, total, q, acc, cnt);
+            pair_sums_s<real, BLOCK>(a.pc0, P, a.pos, a.pol, srun, total, q, acc, cnt);
         else
-            pair_sums(pair_constants(rp), P, a.pos, a.pol, run, total, q, acc, cnt);
+            pair_sums_s<real, BLOCK>(pair_constants(rp), P, a.pos, a.pol, srun, total, q, acc, cnt);
         const real Fxr = acc[0], Fyr = acc[1], Fzr = acc[2];
         const real mxr = acc[3], myr = acc[4], mzr = acc[5];
 
@@ -707,20 +717,25 @@ struct FinArgs {
     int* pending;  // set by k_step, cleared by k_scatter and after a standalone finalize
 };
 
-// One block: replica r's order parameter of `step` into the series; zeroes its accumulators.
+// One block: replica r's order parameter of `step` into the series; zeroes its accumulators. Warp k
+// sums component k over the kPhiCopies copies in int64 (exact, so the order of the additions does
+// not matter); one conversion to double per component.
 template <typename real>
-__device__ void finalize_replica(const FinArgs<real>& f, int r, long long step, double* s) {
-    const int t = threadIdx.x;
-    for (int i = t; i < kPhiCopies * 6; i += blockDim.x) {
-        unsigned long long* p = &f.phi_acc[(size_t)r * kPhiCopies * 6 + i];
-        s[i] = (double)(long long)(*p);
+__device__ void finalize_replica(const FinArgs<real>& f, int r, long long step, long long* s_v) {
+    const int t = threadIdx.x, lane = t & 31, nw = (int)(blockDim.x >> 5);
+    static_assert(kPhiCopies == 32, "one copy per lane");
+    for (int k = t >> 5; k < 6; k += nw) {
+        unsigned long long* p = &f.phi_acc[((size_t)r * kPhiCopies + lane) * 6 + k];
+        long long x = (long long)*p;
         *p = 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) s_v[k] = x;
     }
     __syncthreads();
     if (t == 0) {
-        double v[6] = {0, 0, 0, 0, 0, 0};
-        for (int c = 0; c < kPhiCopies; ++c)
-            for (int k = 0; k < 6; ++k) v[k] += s[c * 6 + k];
+        double v[6];
+        for (int k = 0; k < 6; ++k) v[k] = (double)s_v[k];
         const RepParams<real>& rp = f.reps[r];
         const double inv = 1.0 / rp.phiscale;
         const double phi = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) * inv * rp.inv_n;
@@ -750,7 +765,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(int* __restrict__ count, 
     __shared__ int s_warp[kScanThreads / 32];
     __shared__ int s_base;
     if ((int)blockIdx.x >= n_tiles) {
-        __shared__ double s_fin[kPhiCopies * 6];
+        __shared__ long long s_fin[6];
         if (*fin.pending == 0) return;
         finalize_replica(fin, (int)blockIdx.x - n_tiles, *d_step, s_fin);
         return;
@@ -904,7 +919,7 @@ __global__ void __launch_bounds__(kScanThreads) k_tile_sums(const int* __restric
 // runs past its tiles, for a step that no k_scan has followed yet.
 template <typename real>
 __global__ void k_finalize(const FinArgs<real> f, const long long* d_step) {
-    __shared__ double s[kPhiCopies * 6];
+    __shared__ long long s[6];
     if (*f.pending == 0) return;
     finalize_replica(f, (int)blockIdx.x, *d_step, s);
 }

@@ -51,9 +51,9 @@ constexpr int kRefThreads = 128;       // pair threads per particle
 constexpr int kRefMaxVuv = 32768;    // the dense distance matrix is Vuv^2 doubles (8 GiB at the limit)
 constexpr int kRefMaxParticles = 65536;  // O(N^2) pair loop, as in the reference
 
-// chart bounding box of a face
+// chart bounding box of a face (FP32: it only rules faces out, with a margin)
 struct alignas(16) FaceBox {
-    double u0, u1, v0, v1;
+    float u0, u1, v0, v1;
 };
 
 struct RefP {
@@ -238,44 +238,48 @@ __global__ void __launch_bounds__(kRefThreads) k_ref_flight(int N, RefP p, int V
 
 // One block per particle: the argmin over all faces of the chart point-triangle distance (ties ->
 // lowest face index), then the distance-weighted 3D point and the nearest corner. The argmin is
-// exact, but most faces are ruled out without evaluating the distance: U = the smallest squared
-// distance from the point to a face centroid bounds the minimum from above, and a face whose
-// bounding box lies farther than U (with a relative margin of 1e-6 that covers rounding) cannot
-// be the argmin; the oracle's distance is evaluated for the rest.
+// exact, but most faces are ruled out without evaluating the FP64 distance: the distance from the
+// point to the nearest face centroid bounds the minimum from above, and a face whose bounding box
+// lies farther than that cannot be the argmin. Both are computed in FP32 (GB300's FP64 rate is a
+// small fraction of its FP32 rate); chart coordinates lie in [0, 1], where FP32 rounding moves a
+// distance by less than 3e-7, so a margin of 2e-6 keeps every face that could attain the minimum.
+// The oracle's distance, in FP64, is evaluated for the rest.
 __global__ void __launch_bounds__(kRefLocateThreads) k_ref_locate(int F, const double2* __restrict__ uvv,
                                                                    const int* __restrict__ fuv,
                                                                    const FaceBox* __restrict__ fbox,
-                                                                   const double2* __restrict__ fcen,
+                                                                   const float2* __restrict__ fcen,
                                                                    const double* __restrict__ v3uv,
                                                                    const double2* __restrict__ uv,
                                                                    double* __restrict__ r3d, int* __restrict__ near) {
     __shared__ double s_d[kRefLocateThreads];
     __shared__ int s_f[kRefLocateThreads];
     const int i = blockIdx.x, t = threadIdx.x;
+    __shared__ float s_u[kRefLocateThreads];
     const double2 P = uv[i];
-    double u2 = 1e300;
+    const float pxf = (float)P.x, pyf = (float)P.y;
+    float u2 = 1e30f;
     for (int f = t; f < F; f += kRefLocateThreads) {
-        const double2 c = fcen[f];
-        const double ex = P.x - c.x, ey = P.y - c.y;
-        const double e2 = ex * ex + ey * ey;
+        const float2 c = fcen[f];
+        const float ex = pxf - c.x, ey = pyf - c.y;
+        const float e2 = ex * ex + ey * ey;
         u2 = e2 < u2 ? e2 : u2;
     }
-    s_d[t] = u2;
+    s_u[t] = u2;
     __syncthreads();
     for (int o = kRefLocateThreads / 2; o > 0; o >>= 1) {
-        if (t < o && s_d[t + o] < s_d[t]) s_d[t] = s_d[t + o];
+        if (t < o && s_u[t + o] < s_u[t]) s_u[t] = s_u[t + o];
         __syncthreads();
     }
-    const double keep = s_d[0] * (1.0 + 1e-6) + 1e-24;
-    const bool finite = isfinite(P.x) && isfinite(P.y);
-    __syncthreads();
+    const float kr = sqrtf(s_u[0]) + 2e-6f;
+    const float keep = kr * kr;
+    const bool finite = isfinite(P.x) && isfinite(P.y) && fabs(P.x) < 4.0 && fabs(P.y) < 4.0;
     double best = 1e300;
     int bf = 0x7fffffff;
     for (int f = t; f < F; f += kRefLocateThreads) {
         if (finite) {
             const FaceBox b = fbox[f];
-            const double bx = P.x < b.u0 ? b.u0 - P.x : (P.x > b.u1 ? P.x - b.u1 : 0.0);
-            const double by = P.y < b.v0 ? b.v0 - P.y : (P.y > b.v1 ? P.y - b.v1 : 0.0);
+            const float bx = pxf < b.u0 ? b.u0 - pxf : (pxf > b.u1 ? pxf - b.u1 : 0.0f);
+            const float by = pyf < b.v0 ? b.v0 - pyf : (pyf > b.v1 ? pyf - b.v1 : 0.0f);
             if (bx * bx + by * by > keep) continue;
         }
         const double d = r_tri_dist(P.x, P.y, uvv[fuv[3 * f]], uvv[fuv[3 * f + 1]], uvv[fuv[3 * f + 2]]);
@@ -369,7 +373,7 @@ struct tds_ref_sim {
     double2* uvv = nullptr;
     int* fuv = nullptr;
     FaceBox* fbox = nullptr;  // per face: chart bounding box
-    double2* fcen = nullptr;  // per face: chart centroid
+    float2* fcen = nullptr;   // per face: chart centroid
     double* v3uv = nullptr;
     double2* uv[2] = {nullptr, nullptr};
     int* n[2] = {nullptr, nullptr};
@@ -559,25 +563,25 @@ int tds_ref_create(const tds_mesh* mesh, const double* vertex_dist, const tds_re
     std::vector<double> v3uv((size_t)3 * h.Vuv);
     for (int t = 0; t < h.Vuv; ++t)
         for (int c = 0; c < 3; ++c) v3uv[3 * t + c] = h.v3[3 * h.uv2v[t] + c];
-    std::vector<double> box((size_t)4 * h.F), cen((size_t)2 * h.F);
+    std::vector<float> box((size_t)4 * h.F), cen((size_t)2 * h.F);
     for (int f = 0; f < h.F; ++f) {
         const double* A = &h.uv[2 * (size_t)h.fuv[3 * f]];
         const double* B = &h.uv[2 * (size_t)h.fuv[3 * f + 1]];
         const double* Cc = &h.uv[2 * (size_t)h.fuv[3 * f + 2]];
-        box[4 * f] = std::min(A[0], std::min(B[0], Cc[0]));
-        box[4 * f + 1] = std::max(A[0], std::max(B[0], Cc[0]));
-        box[4 * f + 2] = std::min(A[1], std::min(B[1], Cc[1]));
-        box[4 * f + 3] = std::max(A[1], std::max(B[1], Cc[1]));
-        cen[2 * f] = (A[0] + B[0] + Cc[0]) / 3.0;
-        cen[2 * f + 1] = (A[1] + B[1] + Cc[1]) / 3.0;
+        box[4 * f] = (float)std::min(A[0], std::min(B[0], Cc[0]));
+        box[4 * f + 1] = (float)std::max(A[0], std::max(B[0], Cc[0]));
+        box[4 * f + 2] = (float)std::min(A[1], std::min(B[1], Cc[1]));
+        box[4 * f + 3] = (float)std::max(A[1], std::max(B[1], Cc[1]));
+        cen[2 * f] = (float)((A[0] + B[0] + Cc[0]) / 3.0);
+        cen[2 * f + 1] = (float)((A[1] + B[1] + Cc[1]) / 3.0);
     }
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) rc = TDS_ERR_CUDA;
     if (!rc) rc = ref_alloc(s, &s->D, (size_t)h.Vuv * h.Vuv * sizeof(double));
     if (!rc) rc = ref_alloc(s, &s->uvv, (size_t)h.Vuv * sizeof(double2));
     if (!rc) rc = ref_alloc(s, &s->fuv, (size_t)3 * h.F * sizeof(int));
     if (!rc) rc = ref_alloc(s, &s->v3uv, v3uv.size() * sizeof(double));
-    if (!rc) rc = ref_alloc(s, &s->fbox, box.size() * sizeof(double));
-    if (!rc) rc = ref_alloc(s, &s->fcen, cen.size() * sizeof(double));
+    if (!rc) rc = ref_alloc(s, &s->fbox, box.size() * sizeof(float));
+    if (!rc) rc = ref_alloc(s, &s->fcen, cen.size() * sizeof(float));
     for (int b = 0; b < 2 && !rc; ++b) {
         rc = ref_alloc(s, &s->uv[b], (size_t)N * sizeof(double2));
         if (!rc) rc = ref_alloc(s, &s->n[b], (size_t)N * sizeof(int));
@@ -595,8 +599,8 @@ int tds_ref_create(const tds_mesh* mesh, const double* vertex_dist, const tds_re
             cudaMemcpy(s->uvv, h.uv.data(), (size_t)h.Vuv * sizeof(double2), cudaMemcpyHostToDevice),
             cudaMemcpy(s->fuv, h.fuv.data(), (size_t)3 * h.F * sizeof(int), cudaMemcpyHostToDevice),
             cudaMemcpy(s->v3uv, v3uv.data(), v3uv.size() * sizeof(double), cudaMemcpyHostToDevice),
-            cudaMemcpy(s->fbox, box.data(), box.size() * sizeof(double), cudaMemcpyHostToDevice),
-            cudaMemcpy(s->fcen, cen.data(), cen.size() * sizeof(double), cudaMemcpyHostToDevice),
+            cudaMemcpy(s->fbox, box.data(), box.size() * sizeof(float), cudaMemcpyHostToDevice),
+            cudaMemcpy(s->fcen, cen.data(), cen.size() * sizeof(float), cudaMemcpyHostToDevice),
             cudaMemset(s->rdot, 0, (size_t)N * sizeof(double2)),
             cudaMemset(s->cnt, 0, (size_t)N * sizeof(int)),
             cudaMemset(s->status, 0, sizeof(int))};

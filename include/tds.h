@@ -92,7 +92,7 @@ int tds_ensemble_create(const tds_mesh* mesh, int n_replicas, const int* n_parti
  * cells_per_particle: a replica's cell size is r_max * 2^k for the smallest k whose surface-cell
  *   count is <= max(64, cells_per_particle * N_r) (small replicas on a large surface take
  *   coarser cells); default 4.
- * step_block: threads per block of the step kernel, 128 or 256 (default 256).
+ * step_block: threads per block of the step kernel, 128 or 256 (default 128).
  * graph_steps: steps per captured CUDA graph, even, 2..256 (default 16). */
 typedef struct tds_tuning {
     double cells_per_particle;

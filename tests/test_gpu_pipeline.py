@@ -74,3 +74,23 @@ def test_get_state_async_checks_output_arrays(tg, mesh_l4):
     o["uv"] = np.zeros((100, 2), np.float32)
     with pytest.raises(ValueError):
         sim.get_state_async(o)
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_state_without_r3d_is_the_same_state(tg, mesh_l4, precision):
+    """The 3D position is the face's chart map of the chart position: a state given as (uv, theta,
+    face) alone loads to the same device state, bit for bit, as one given with r3d, and the next
+    steps agree exactly (the end-to-end bench uploads the state that way)."""
+    n = 1500
+    (x,) = _inputs(tg, mesh_l4, n, precision, 1)
+    a = tg.Simulation(mesh_l4, tg.Params(), n, seed=5, precision=precision)
+    b = tg.Simulation(mesh_l4, tg.Params(), n, seed=5, precision=precision)
+    a.set_state(**x)
+    b.set_state(x["uv"], x["theta"], x["face"])
+    sa, sb = a.get_state(), b.get_state()
+    np.testing.assert_array_equal(sa["r3d"], sb["r3d"])
+    a.step(3)
+    b.step(3)
+    sa, sb = a.get_state(), b.get_state()
+    for key in sa:
+        np.testing.assert_array_equal(sa[key], sb[key])
