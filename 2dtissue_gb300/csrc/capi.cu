@@ -912,7 +912,6 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp, tds_adjoint_result* res)
     a.aF = aF, a.aM = aM, a.aP = aP;
     a.gpar = gpar;
     a.N = s->N;
-    const int nb = (s->N + 255) / 256;
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int t0 = seg * K, t1 = std::min(T, t0 + K);
         if (seg != nseg - 1) {  // recompute the segment from its checkpoint, storing each step
@@ -934,8 +933,8 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp, tds_adjoint_result* res)
             a.r_target = (t == T - 1 && rtgt && sp->w_pos > 0) ? rtgt : nullptr;
             a.lam_in = lam[cur];
             a.lam_out = lam[cur ^ 1];
-            tdsk::k_adj_a<real><<<nb, 256, 0, s->stream>>>(a);
-            tdsk::k_adj_b<real><<<nb, 256, 0, s->stream>>>(a);
+            tdsk::k_adj_a<real><<<(s->N + tdsk::kAdjThreads - 1) / tdsk::kAdjThreads, tdsk::kAdjThreads, 0, s->stream>>>(a);
+            tdsk::k_adj_b<real><<<(s->N + tdsk::kAdjThreads - 1) / tdsk::kAdjThreads, tdsk::kAdjThreads, 0, s->stream>>>(a);
             cur ^= 1;
         }
     }
