@@ -108,6 +108,7 @@ def lib(build_if_missing=True):
     L.tds_get_tuning.argtypes = [VP, P(_Tuning)]
     L.tds_autotune.argtypes = [VP, I, VP, VP, C.c_uint64, I, I, P(_Tuning), P(D)]
     L.tds_adjoint_run.argtypes = [VP, P(_AdjSpec), P(_AdjResult)]
+    L.tds_adjoint_release.argtypes = [VP]
     L.tds_get_order_parameter.argtypes = [VP, VP, VP, I, P(I)]
     L.tds_get_step.argtypes = [VP, P(C.c_int64)]
     L.tds_get_status.argtypes = [VP, P(I)]
@@ -363,6 +364,10 @@ class Simulation:
         res = _AdjResult(0.0, _ptr(dp), _ptr(duv), _ptr(dth), 0)
         self._check(lib().tds_adjoint_run(self.h, C.byref(spec), C.byref(res)))
         return dict(loss=res.loss, d_params=dp[:, :7], d_uv0=duv, d_theta0=dth, checkpoint_stride=res.checkpoint_stride)
+
+    def adjoint_release(self):
+        """Frees the adjoint's work memory that the handle keeps between adjoint() calls."""
+        self._check(lib().tds_adjoint_release(self.h))
 
     def get_state_noalloc(self, out=None):
         """Same as get_state, staged in the library's fixed device array (no device allocation;

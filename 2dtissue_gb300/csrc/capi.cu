@@ -119,6 +119,10 @@ struct tds_sim {
     double cells_per_particle = 4.0;  // cell-level rule (tuning): finest level with C <= max(64, this * N_r)
     double origin[3] = {0, 0, 0};
     std::vector<void*> allocs;
+    // adjoint work memory (checkpoints, the per-step store, adjoint buffers): one device block kept
+    // between tds_adjoint_run calls and grown when a call needs more (tds_adjoint_release frees it)
+    void* adj_ws = nullptr;
+    size_t adj_ws_bytes = 0;
     // per-kernel event timing
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -597,6 +601,22 @@ struct Arena {
     }
 };
 
+// Sub-buffers carved from one block (256-byte aligned). In measuring mode it only adds up the
+// bytes and hands out non-null placeholders.
+struct Carve {
+    char* base = nullptr;
+    size_t cap = 0, used = 0;
+    bool measure = true;
+    template <typename T>
+    T* get(size_t n) {
+        const size_t bytes = (std::max<size_t>(n * sizeof(T), 16) + 255) & ~(size_t)255;
+        const size_t off = used;
+        used += bytes;
+        if (measure) return reinterpret_cast<T*>((size_t)256 + off);
+        return used <= cap ? reinterpret_cast<T*>(base + off) : nullptr;
+    }
+};
+
 // Loads the state waiting in the input staging (k_load_state computes polarity, cell keys and
 // counts) on the compute stream; per-tile counts for the next scan.
 template <typename real>
@@ -748,7 +768,7 @@ struct Snapshot {
     int* count = nullptr;
     int* tile_sum = nullptr;
     long long* d_step = nullptr;
-    bool alloc(Arena& A, size_t N, size_t M, int n_tiles) {
+    bool alloc(Carve& A, size_t N, size_t M, int n_tiles) {
         pos = A.get<R4<real>>(N), pol = A.get<R4<real>>(N), uv = A.get<R2<real>>(N);
         ids = A.get<int>(N), key = A.get<int>(N), count = A.get<int>(M), tile_sum = A.get<int>(2 * (size_t)n_tiles);
         d_step = A.get<long long>(1);
@@ -775,6 +795,43 @@ void snapshot_copy(tds_sim* s, const Snapshot<real>& x, bool take) {
     cp(x.d_step, s->d_step, sizeof(long long));
 }
 
+// The two captured K-step segments of an adjoint run (without and with the per-step store).
+template <typename real>
+struct SegGraphs {
+    tds_sim* s;
+    int K;
+    const StepHooks* hk;
+    const StepStore* store;
+    cudaGraphExec_t g[2] = {nullptr, nullptr};
+    SegGraphs(tds_sim* s_, int K_, const StepHooks* hk_, const StepStore* store_) : s(s_), K(K_), hk(hk_), store(store_) {}
+    ~SegGraphs() {
+        for (cudaGraphExec_t x : g)
+            if (x) cudaGraphExecDestroy(x);
+    }
+    int launch(bool stored) {
+        cudaGraphExec_t& x = g[stored ? 1 : 0];
+        if (!x) {
+            cudaGraph_t graph = nullptr;
+            CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+            StepHooks h = *hk;
+            for (int k = 0; k < K; ++k) {
+                h.store = stored ? &store[k] : nullptr;
+                launch_one_step<real>(s, nullptr, &h);
+            }
+            const cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+            if (e != cudaSuccess) return fail(s, TDS_ERR_CUDA, std::string("adjoint segment capture: ") + cudaGetErrorString(e));
+            const cudaError_t e2 = cudaGraphInstantiate(&x, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e2 != cudaSuccess) {
+                x = nullptr;
+                return fail(s, TDS_ERR_CUDA, std::string("adjoint segment graph: ") + cudaGetErrorString(e2));
+            }
+        }
+        CK(cudaGraphLaunch(x, s->stream));
+        return TDS_OK;
+    }
+};
+
 template <typename real>
 int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp, tds_adjoint_result* res) {
     const int T = sp->n_steps;
@@ -793,6 +850,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp, tds_adjoint_result* res)
     if (K <= 0) {
         size_t fr = 0, tot = 0;
         CK(cudaMemGetInfo(&fr, &tot));
+        fr += s->adj_ws_bytes;  // the cached work block is reused (or freed and replaced)
         const double budget = fr > b_fixed ? 0.8 * (double)(fr - b_fixed) : 0.0;
         for (int k = T; k >= 1; --k) {
             const double need = (double)((T + k - 1) / k) * (double)b_snap + (double)k * (double)b_store;
@@ -805,37 +863,57 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp, tds_adjoint_result* res)
     }
     K = std::min(K, T);
     const int nseg = (T + K - 1) / K;
-    const int last0 = (nseg - 1) * K;
 
-    Arena A;
     std::vector<Snapshot<real>> snaps(nseg);
     Snapshot<real> fin;
-    for (auto& x : snaps)
-        if (!x.alloc(A, N, M, s->n_tiles)) return fail(s, TDS_ERR_NOMEM, "adjoint: checkpoint allocation");
-    if (!fin.alloc(A, N, M, s->n_tiles)) return fail(s, TDS_ERR_NOMEM, "adjoint: checkpoint allocation");
     std::vector<StepStore> store(K);
-    for (auto& x : store) {
-        x.pos = A.get<R4<real>>(N), x.pol = A.get<R4<real>>(N), x.uv = A.get<R2<real>>(N);
-        x.ids = A.get<int>(N), x.key = A.get<int>(N), x.start = A.get<int>(M + 1);
-        if (!(x.pos && x.pol && x.uv && x.ids && x.key && x.start))
-            return fail(s, TDS_ERR_NOMEM, "adjoint: segment store allocation");
-        const int nN = s->N;  // the scan writes start[0..M); start[M] = N stays
-        CK(cudaMemcpy(x.start + M, &nN, sizeof(int), cudaMemcpyHostToDevice));
+    real* lam[2] = {nullptr, nullptr};
+    R4<real>*aF = nullptr, *aM = nullptr, *aP = nullptr;
+    double *gpar = nullptr, *phisum = nullptr, *phibar = nullptr, *rtgt = nullptr, *d_gp = nullptr;
+    int *d_off = nullptr, *d_cnt = nullptr;
+    // all work buffers come from one block: measured first, then carved
+    auto carve = [&](Carve& A) -> bool {
+        bool ok = true;
+        for (auto& x : snaps) ok = x.alloc(A, N, M, s->n_tiles) && ok;
+        ok = fin.alloc(A, N, M, s->n_tiles) && ok;
+        for (auto& x : store) {
+            x.pos = A.get<R4<real>>(N), x.pol = A.get<R4<real>>(N), x.uv = A.get<R2<real>>(N);
+            x.ids = A.get<int>(N), x.key = A.get<int>(N), x.start = A.get<int>(M + 1);
+            ok = ok && x.pos && x.pol && x.uv && x.ids && x.key && x.start;
+        }
+        lam[0] = A.get<real>(3 * N), lam[1] = A.get<real>(3 * N);
+        aF = A.get<R4<real>>(N), aM = A.get<R4<real>>(N), aP = A.get<R4<real>>(N);
+        gpar = A.get<double>(N * tdsk::kGPar);
+        phisum = A.get<double>((size_t)T * R * 6);
+        phibar = A.get<double>((size_t)T * R);
+        rtgt = sp->r3d_target ? A.get<double>(3 * N) : nullptr;
+        d_off = A.get<int>(R), d_cnt = A.get<int>(R);
+        d_gp = A.get<double>(R * tdsk::kGPar);
+        return ok && lam[0] && lam[1] && aF && aM && aP && gpar && phisum && phibar && d_off && d_cnt && d_gp &&
+               (!sp->r3d_target || rtgt);
+    };
+    {
+        Carve m;
+        carve(m);
+        if (m.used > s->adj_ws_bytes) {
+            if (s->adj_ws) cudaFree(s->adj_ws);
+            s->adj_ws = nullptr, s->adj_ws_bytes = 0;
+            void* q = nullptr;
+            if (cudaMalloc(&q, m.used) != cudaSuccess) {
+                cudaGetLastError();
+                return fail(s, TDS_ERR_NOMEM, "adjoint: work memory allocation");
+            }
+            s->adj_ws = q, s->adj_ws_bytes = m.used;
+        }
+        Carve c;
+        c.base = (char*)s->adj_ws, c.cap = s->adj_ws_bytes, c.measure = false;
+        if (!carve(c)) return fail(s, TDS_ERR_NOMEM, "adjoint: work memory carving");
     }
-    real* lam[2] = {A.get<real>(3 * N), A.get<real>(3 * N)};
-    R4<real>* aF = A.get<R4<real>>(N);
-    R4<real>* aM = A.get<R4<real>>(N);
-    R4<real>* aP = A.get<R4<real>>(N);
-    double* gpar = A.get<double>(N * tdsk::kGPar);
-    double* phisum = A.get<double>((size_t)T * R * 6);
-    double* phibar = A.get<double>((size_t)T * R);
-    double* rtgt = sp->r3d_target ? A.get<double>(3 * N) : nullptr;
-    int* d_off = A.get<int>(R);
-    int* d_cnt = A.get<int>(R);
-    double* d_gp = A.get<double>(R * tdsk::kGPar);
-    if (!(lam[0] && lam[1] && aF && aM && aP && gpar && phisum && phibar && d_off && d_cnt && d_gp) ||
-        (sp->r3d_target && !rtgt))
-        return fail(s, TDS_ERR_NOMEM, "adjoint: work buffer allocation");
+    {
+        const int nN = s->N;  // the scan writes start[0..M); start[M] = N stays
+        for (auto& x : store) CK(cudaMemcpyAsync(x.start + M, &nN, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
     if ((rc = ensure_series(s, s->step + T))) return rc;
     free_graphs(s);
 
@@ -843,10 +921,23 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp, tds_adjoint_result* res)
     const long long t_base = s->step;
     StepHooks hk;
     hk.phisum = phisum, hk.phisum_base = t_base, hk.phisum_cap = T;
-    for (int t = 0; t < T; ++t) {
-        if (t % K == 0) snapshot_copy<real>(s, snaps[t / K], true);
-        hk.store = t >= last0 ? &store[t - last0] : nullptr;
-        launch_one_step<real>(s, nullptr, &hk);
+    // A full segment's K steps are the same launches every time (the store slots are reused by
+    // each segment, and the step counter and the order-parameter index live on the device), so
+    // they are captured once as a CUDA graph without the store (the forward's earlier segments)
+    // and once with it (the forward's last segment and every recomputed segment). On a small
+    // system the step is launch-bound and the graphs remove the launch gaps.
+    SegGraphs<real> sg(s, K, &hk, store.data());
+    auto run_segment = [&](int t0, int t1, bool stored) -> int {
+        if (t1 - t0 == K && !s->timing) return sg.launch(stored);
+        for (int t = t0; t < t1; ++t) {
+            hk.store = stored ? &store[t - t0] : nullptr;
+            launch_one_step<real>(s, nullptr, &hk);
+        }
+        return TDS_OK;
+    };
+    for (int seg = 0; seg < nseg; ++seg) {
+        snapshot_copy<real>(s, snaps[seg], true);
+        if ((rc = run_segment(seg * K, std::min(T, seg * K + K), seg == nseg - 1))) return rc;
     }
     flush_finalize<real>(s, &hk);
     CK(cudaGetLastError());
@@ -916,11 +1007,8 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp, tds_adjoint_result* res)
         const int t0 = seg * K, t1 = std::min(T, t0 + K);
         if (seg != nseg - 1) {  // recompute the segment from its checkpoint, storing each step
             snapshot_copy<real>(s, snaps[seg], false);
-            StepHooks rk;
-            for (int t = t0; t < t1; ++t) {
-                rk.store = &store[t - t0];
-                launch_one_step<real>(s, nullptr, &rk);
-            }
+            // (the order-parameter sums of these steps are written again, with the same values)
+            if ((rc = run_segment(t0, t1, true))) return rc;
             flush_finalize<real>(s);  // the next restore must not finalize this segment's last step
         }
         for (int t = t1 - 1; t >= t0; --t) {
@@ -1347,6 +1435,16 @@ int tds_set_params(tds_sim* s, const tds_params* params) {
     return s->precision == 32 ? set_params<float>(s, params) : set_params<double>(s, params);
 }
 
+int tds_adjoint_release(tds_sim* s) {
+    if (!s) return TDS_ERR_ARG;
+    if (s->adj_ws) {
+        if (int rc = sync_all(s)) return rc;
+        cudaFree(s->adj_ws);
+        s->adj_ws = nullptr, s->adj_ws_bytes = 0;
+    }
+    return TDS_OK;
+}
+
 int tds_adjoint_run(tds_sim* s, const tds_adjoint_spec* spec, tds_adjoint_result* out) {
     if (!s || !spec || !out) return TDS_ERR_ARG;
     return s->precision == 32 ? adjoint_run<float>(s, spec, out) : adjoint_run<double>(s, spec, out);
@@ -1428,6 +1526,7 @@ void tds_destroy(tds_sim* s) {
     for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
     free_graphs(s);
     for (void* p : s->allocs) cudaFree(p);
+    if (s->adj_ws) cudaFree(s->adj_ws);
     if (s->series) cudaFree(s->series);
     if (s->noise) cudaFree(s->noise);
     for (cudaEvent_t e : {s->ev_in_ready[0], s->ev_in_free[0], s->ev_out_ready[0], s->ev_out_free[0],

@@ -186,6 +186,10 @@ typedef struct tds_adjoint_result {
  * recomputing each segment from its checkpoint with every step's sorted state kept, and two
  * kernels per step. */
 int tds_adjoint_run(tds_sim* sim, const tds_adjoint_spec* spec, tds_adjoint_result* out);
+/* tds_adjoint_run keeps its work memory (checkpoints, the per-step store: up to 80% of the free
+ * device memory) in the handle between calls, so that repeated runs (parameter inference) do not map
+ * and unmap it each time; this frees it now (tds_destroy frees it too). */
+int tds_adjoint_release(tds_sim* sim);
 /* Per-kernel CUDA-event timing of directly launched steps (graphs are not used while enabled).
  * tds_kernel_times returns, per kernel (0 scan + order-parameter finalize, 1 scatter, 2 order, 3 step,
  * 4 standalone finalize before a series read), the

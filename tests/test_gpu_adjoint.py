@@ -197,3 +197,29 @@ def test_autograd_function(tg, mesh_l4):
     np.testing.assert_allclose(loss.item(), out["loss"], rtol=1e-12)
     np.testing.assert_allclose(params.grad.numpy()[0], 2.0 * out["d_params"][0], rtol=1e-12)
     np.testing.assert_allclose(uv0.grad.numpy(), 2.0 * out["d_uv0"], rtol=1e-12, atol=1e-300)
+
+
+def test_repeated_adjoint_calls_reuse_the_work_memory(tg, mesh_l4):
+    """The handle keeps the adjoint's work memory between calls: a repeated call, a longer call
+    (the block grows) and a call after tds_adjoint_release give the same gradients as the first.
+    No noise (eta = 0): each call starts from the same state but at a later step counter."""
+    sim = _start(tg, mesh_l4, 32, params=tg.Params(eta=0.0))
+    s0 = sim.get_state()
+
+    def run(steps):
+        sim.set_state(s0["uv"], s0["theta"], s0["face"])
+        return sim.adjoint(steps, r3d_target=s0["r3d"], w_pos=1.0, phi_target=np.zeros(steps), w_phi=1.0,
+                           checkpoint_stride=2)
+
+    first = run(T)
+    again = run(T)
+    longer = run(T + 4)
+    after_longer = run(T)
+    sim.adjoint_release()
+    released = run(T)
+    assert longer["d_params"].shape == first["d_params"].shape
+    for o in (again, after_longer, released):
+        for k in ("loss", "d_uv0", "d_theta0"):
+            np.testing.assert_array_equal(first[k], o[k])
+        # all but eta: dL/d eta weighs the noise draws, which follow the step counter
+        np.testing.assert_array_equal(first["d_params"][:, :6], o["d_params"][:, :6])
