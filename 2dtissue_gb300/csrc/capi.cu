@@ -11,6 +11,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/tds.h"
 #include "adjoint.cuh"
 #include "geometry.hpp"
@@ -29,6 +31,13 @@ struct tds_mesh {
 namespace {
 
 thread_local std::string g_mesh_err;
+
+// NVTX range over a library phase (header-only NVTX v3: a no-op unless a profiler is attached), so
+// that profiles of a caller's program show the steps, state transfers and adjoint passes by name.
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+};
 
 int mesh_fail(const std::string& msg) {
     g_mesh_err = msg;
@@ -535,6 +544,7 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
 
 template <typename real>
 int run_steps(tds_sim* s, int n, const double* noise_host, bool sync = true) {
+    Range range("tds_step");
     int rc;
     if ((rc = ensure_series(s, s->step + n))) return rc;
     if (noise_host) {
@@ -643,6 +653,7 @@ int load_from_staging(tds_sim* s, int b, bool has_face, bool has_r3d, bool sync)
 // upload waits until the previous load has consumed the staging.
 template <typename real>
 int load_state(tds_sim* s, const tds_state_view* in, bool sync) {
+    Range range("tds_set_state");
     const size_t N = (size_t)s->N;
     if (!in || !in->uv || !in->theta) return fail(s, TDS_ERR_ARG, "set_state needs uv and theta");
     if (in->face) {
@@ -707,6 +718,7 @@ int start_device(tds_sim* s) {
 // download stream. The gather waits until the previous download has left the staging.
 template <typename real>
 int save_state(tds_sim* s, tds_state_view* out, bool sync) {
+    Range range("tds_get_state");
     const size_t N = (size_t)s->N;
     const int b = s->out_next;
     s->out_next ^= 1;
@@ -834,6 +846,7 @@ struct SegGraphs {
 
 template <typename real>
 int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp, tds_adjoint_result* res) {
+    Range range("tds_adjoint_run");
     const int T = sp->n_steps;
     if (T < 1) return fail(s, TDS_ERR_ARG, "adjoint: n_steps must be >= 1");
     if (!(sp->w_pos >= 0 && sp->w_phi >= 0)) return fail(s, TDS_ERR_ARG, "adjoint: weights must be >= 0");
@@ -935,11 +948,14 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp, tds_adjoint_result* res)
         }
         return TDS_OK;
     };
-    for (int seg = 0; seg < nseg; ++seg) {
-        snapshot_copy<real>(s, snaps[seg], true);
-        if ((rc = run_segment(seg * K, std::min(T, seg * K + K), seg == nseg - 1))) return rc;
+    {
+        Range fwd("adjoint forward");
+        for (int seg = 0; seg < nseg; ++seg) {
+            snapshot_copy<real>(s, snaps[seg], true);
+            if ((rc = run_segment(seg * K, std::min(T, seg * K + K), seg == nseg - 1))) return rc;
+        }
+        flush_finalize<real>(s, &hk);
     }
-    flush_finalize<real>(s, &hk);
     CK(cudaGetLastError());
     s->step += T;
     snapshot_copy<real>(s, fin, true);
@@ -984,6 +1000,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp, tds_adjoint_result* res)
     }
 
     // ---- reverse sweep ----
+    Range rev("adjoint reverse");
     CK(cudaMemsetAsync(lam[0], 0, 3 * N * sizeof(real), s->stream));
     CK(cudaMemsetAsync(gpar, 0, N * tdsk::kGPar * sizeof(double), s->stream));
     int cur = 0;
