@@ -249,13 +249,17 @@ template <typename real>
 __device__ int locate(const real* rec, const int4* adj, int G, const int* bs, const int* bf, real px, real py,
                       int f_old, int& mode) {
     mode = 0;
-    if (min_edge(rec + (size_t)f_old * kRec, px, py) > (real)0) return f_old;
+    real e[3];
+    edge_values(rec + (size_t)f_old * kRec, px, py, e);
+    if (fmin(e[0], fmin(e[1], e[2])) > (real)0) return f_old;
     if (adj) {
+        // the neighbour across edge k can strictly contain p only if p lies strictly outside
+        // that edge (shared edges give exactly negated values), so only those are tested
         const int4 A = adj[f_old];
         const int nb[3] = {A.x, A.y, A.z};
 #pragma unroll
         for (int k = 0; k < 3; ++k)
-            if (nb[k] >= 0 && min_edge(rec + (size_t)nb[k] * kRec, px, py) > (real)0) return nb[k];
+            if (e[k] < (real)0 && nb[k] >= 0 && min_edge(rec + (size_t)nb[k] * kRec, px, py) > (real)0) return nb[k];
     }
     const int bx = bin_coord(px, G), by = bin_coord(py, G);
     const int b = by * G + bx;
