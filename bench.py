@@ -639,6 +639,26 @@ def run_ref(args):
     print(json.dumps(line), flush=True)
 
 
+def run_profile_adjoint(args):
+    """Minimal driver for ncu: the 512-replica bumpy-sphere ensemble of the batched-adjoint workload,
+    placed, then one adjoint run of `steps` steps (one stored segment); no timing."""
+    import torch
+    tg = importlib.import_module("2dtissue_gb300")
+    mesh = tg.Mesh.bumpy_sphere(6, 0.2, 5.0)
+    rng = np.random.default_rng(5)
+    R = 512
+    ns = [int(x) for x in rng.integers(1000, 20001, size=R)]
+    ps = [tg.Params(v0=float(rng.uniform(0.5, 1.5)), k_rep=float(rng.uniform(5, 20)), tau=float(rng.uniform(0.5, 2)),
+                    eta=float(rng.uniform(0.1, 1.0))) for _ in range(R)]
+    sim = tg.Simulation(mesh, ps, ns, seed=1, precision=32)
+    sim.start()
+    s0 = sim.get_state()
+    T = args.steps
+    sim.adjoint(T, r3d_target=s0["r3d"], w_pos=1.0, phi_target=np.full((T, R), 0.05), w_phi=1.0)
+    torch.cuda.synchronize()
+    sim.close()
+
+
 def run_profile(args):
     """Minimal driver for ncu: the 1M-particle system, `warmup` steps, then `steps` steps; no timing."""
     import torch
@@ -670,7 +690,7 @@ def main():
     if args.steps is None:
         args.steps = {"plain": 500, "ensemble": 50, "adjoint": 2000, "adjoint_batched": 500, "ref": 50}[args.workload]
     if args.profile:
-        return run_profile(args)
+        return run_profile_adjoint(args) if args.workload == "adjoint_batched" else run_profile(args)
     if args.workload == "ensemble" and args.impl != "reference":
         return run_ensemble(args)
     if args.workload == "adjoint" and args.impl != "reference":
