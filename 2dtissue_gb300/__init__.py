@@ -49,6 +49,13 @@ class _AdjResult(C.Structure):
                 ("checkpoint_stride", C.c_int)]
 
 
+# the reference's Particle record (src/simulation/Struct.h:9-29) as tds_get_particles fills it
+PARTICLE_DTYPE = np.dtype({"names": ["x_UV", "y_UV", "x_velocity_UV", "y_velocity_UV", "alignment_UV",
+                                     "compass_north_pole_UV", "compass_south_pole_UV", "x_3D", "y_3D", "z_3D",
+                                     "neighbor_count"],
+                           "formats": ["<f8"] * 10 + ["<i4"],
+                           "offsets": [8 * k for k in range(10)] + [80], "itemsize": 88})
+
 # order of the parameter gradients returned by the adjoint
 GRAD_PARAMS = ("k_rep", "k_adh", "v0", "mu", "tau", "align", "eta")
 
@@ -100,6 +107,7 @@ def lib(build_if_missing=True):
     L.tds_set_state.argtypes = [VP, P(_StateView)]
     L.tds_get_state.argtypes = [VP, P(_StateView)]
     L.tds_get_state_noalloc.argtypes = [VP, P(_StateView)]
+    L.tds_get_particles.argtypes = [VP, VP]
     L.tds_set_state_async.argtypes = [VP, P(_StateView)]
     L.tds_get_state_async.argtypes = [VP, P(_StateView)]
     L.tds_sync.argtypes = [VP]
@@ -368,6 +376,12 @@ class Simulation:
     def adjoint_release(self):
         """Frees the adjoint's work memory that the handle keeps between adjoint() calls."""
         self._check(lib().tds_adjoint_release(self.h))
+
+    def get_particles(self):
+        """update()'s Particle records (numpy structured array, PARTICLE_DTYPE), packed on the device."""
+        out = np.zeros(self.N, PARTICLE_DTYPE)
+        self._check(lib().tds_get_particles(self.h, out.ctypes.data))
+        return out
 
     def get_state_noalloc(self, out=None):
         """Same as get_state, staged in the library's fixed device array (no device allocation;

@@ -132,6 +132,7 @@ struct tds_sim {
     // between tds_adjoint_run calls and grown when a call needs more (tds_adjoint_release frees it)
     void* adj_ws = nullptr;
     size_t adj_ws_bytes = 0;
+    tds_particle* pk = nullptr;  // Particle records staged for tds_get_particles (allocated on first use)
     // per-kernel event timing
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -747,6 +748,29 @@ int save_state(tds_sim* s, tds_state_view* out, bool sync) {
     if (out->nbr_count) CK(cudaMemcpyAsync(out->nbr_count, d_cnt, N * sizeof(int), cudaMemcpyDeviceToHost, d));
     CK(cudaEventRecord(s->ev_out_free[b], d));
     if (sync) CK(cudaStreamSynchronize(d));
+    return TDS_OK;
+}
+
+// update()'s Particle records, packed on the device (id order) and copied in one transfer.
+template <typename real>
+int get_particles(tds_sim* s, tds_particle* out) {
+    Range range("tds_get_particles");
+    const size_t N = (size_t)s->N;
+    if (!s->pk) {
+        void* q = nullptr;
+        if (cudaMalloc(&q, N * sizeof(tds_particle)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(s, TDS_ERR_NOMEM, "get_particles: staging allocation");
+        }
+        s->pk = (tds_particle*)q;
+    }
+    const int c = s->cur;
+    tdsk::k_pack_particles<real><<<(s->N + 255) / 256, 256, 0, s->stream>>>(
+        (const R4<real>*)s->pos[c], (const R2<real>*)s->uv[c], s->ids[c], (const R2<real>*)s->vel[c], s->cnt[c],
+        (const RepParams<real>*)s->reps, s->local_bits, s->pk, s->N);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, s->pk, N * sizeof(tds_particle), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
     return TDS_OK;
 }
 
@@ -1467,6 +1491,11 @@ int tds_adjoint_run(tds_sim* s, const tds_adjoint_spec* spec, tds_adjoint_result
     return s->precision == 32 ? adjoint_run<float>(s, spec, out) : adjoint_run<double>(s, spec, out);
 }
 
+int tds_get_particles(tds_sim* s, tds_particle* out) {
+    if (!s || !out) return TDS_ERR_ARG;
+    return s->precision == 32 ? get_particles<float>(s, out) : get_particles<double>(s, out);
+}
+
 int tds_get_state_noalloc(tds_sim* s, tds_state_view* out) {
     if (!s || !out) return TDS_ERR_ARG;
     return s->precision == 32 ? save_state_noalloc<float>(s, out) : save_state_noalloc<double>(s, out);
@@ -1544,6 +1573,7 @@ void tds_destroy(tds_sim* s) {
     free_graphs(s);
     for (void* p : s->allocs) cudaFree(p);
     if (s->adj_ws) cudaFree(s->adj_ws);
+    if (s->pk) cudaFree(s->pk);
     if (s->series) cudaFree(s->series);
     if (s->noise) cudaFree(s->noise);
     for (cudaEvent_t e : {s->ev_in_ready[0], s->ev_in_free[0], s->ev_out_ready[0], s->ev_out_free[0],

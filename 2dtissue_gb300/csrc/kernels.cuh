@@ -35,6 +35,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/tds.h"
 #include "philox.cuh"
 
 namespace tdsk {
@@ -947,6 +948,28 @@ __global__ void k_gather_state(const R4<real>* pos, const R4<real>* pol, const R
     const R2<real> V = vel[s];
     o_vel[2 * i] = V.x, o_vel[2 * i + 1] = V.y;
     o_cnt[i] = cnt[s];
+}
+
+// State (physical order) -> the reference's Particle records in id order (tds_particle, 88 bytes:
+// ten doubles and the neighbour count). The angle in degrees is (theta * 180) / pi, as the C++
+// facade writes it.
+template <typename real>
+__global__ void k_pack_particles(const R4<real>* pos, const R2<real>* uv, const int* ids, const R2<real>* vel,
+                                 const int* cnt, const RepParams<real>* reps, int local_bits, tds_particle* out, int N) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    const unsigned id = (unsigned)ids[s];
+    const int i = reps[id >> local_bits].off + (int)(id & ((1u << local_bits) - 1u));
+    const R4<real> P = pos[s];
+    const R2<real> U = uv[s], V = vel[s];
+    tds_particle q;
+    q.x_UV = U.x, q.y_UV = U.y;
+    q.x_velocity_UV = V.x, q.y_velocity_UV = V.y;
+    q.alignment_UV = __ddiv_rn(__dmul_rn((double)P.w, 180.0), 3.14159265358979323846);
+    q.compass_north_pole_UV = 0.0, q.compass_south_pole_UV = 0.0;
+    q.x_3D = P.x, q.y_3D = P.y, q.z_3D = P.z;
+    q.neighbor_count = cnt[s];
+    out[i] = q;
 }
 
 // Loads a state given in id order (double) into slots = global index; locates faces that are

@@ -10,6 +10,7 @@
 //   * Kafka/SQLite sinks and the particle "Innenleben" are not part of this path.
 #pragma once
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <filesystem>
 #include <fstream>
@@ -35,6 +36,13 @@ struct System {
     double order_parameter;
     std::vector<Particle> particles;
 };
+
+// The C-ABI's record has the same fields in the same order: update() receives the device-packed
+// records straight into System::particles.
+static_assert(sizeof(Particle) == sizeof(tds_particle), "Particle and tds_particle must have one layout");
+static_assert(offsetof(Particle, alignment_UV) == offsetof(tds_particle, alignment_UV), "layout");
+static_assert(offsetof(Particle, x_3D) == offsetof(tds_particle, x_3D), "layout");
+static_assert(offsetof(Particle, neighbor_count) == offsetof(tds_particle, neighbor_count), "layout");
 
 class Tissue2D {
   public:
@@ -66,8 +74,6 @@ class Tissue2D {
             tds_mesh_destroy(mesh_);
             throw std::runtime_error("tds_create failed (code " + std::to_string(rc) + ")");
         }
-        uv_.resize(2 * (size_t)n_), th_.resize(n_), r3_.resize(3 * (size_t)n_), vel_.resize(2 * (size_t)n_);
-        face_.resize(n_), cnt_.resize(n_);
     }
     Tissue2D(const Tissue2D&) = delete;
     Tissue2D& operator=(const Tissue2D&) = delete;
@@ -79,8 +85,7 @@ class Tissue2D {
     void start() { check(tds_start(sim_)); }
 
     System update() {
-        tds_state_view v{uv_.data(), th_.data(), face_.data(), r3_.data(), vel_.data(), cnt_.data()};
-        check(tds_update(sim_, &v));
+        check(tds_step(sim_, 1, nullptr));
         ++current_step_;
         System sys;
         int ns = 0;
@@ -88,15 +93,8 @@ class Tissue2D {
         check(tds_get_order_parameter(sim_, phi.data(), nullptr, (int)phi.size(), &ns));
         sys.order_parameter = ns > 0 ? phi[ns - 1] : 0.0;
         sys.particles.resize(n_);
-        for (int i = 0; i < n_; ++i) {
-            Particle& q = sys.particles[i];
-            q.x_UV = uv_[2 * i], q.y_UV = uv_[2 * i + 1];
-            q.x_velocity_UV = vel_[2 * i], q.y_velocity_UV = vel_[2 * i + 1];
-            q.alignment_UV = th_[i] * 180.0 / M_PI;
-            q.x_3D = r3_[3 * i], q.y_3D = r3_[3 * i + 1], q.z_3D = r3_[3 * i + 2];
-            q.neighbor_count = cnt_[i];
-        }
-        if (save_data_) save_our_data();
+        check(tds_get_particles(sim_, reinterpret_cast<tds_particle*>(sys.particles.data())));
+        if (save_data_) save_our_data(sys.particles);
         return sys;
     }
 
@@ -117,19 +115,17 @@ class Tissue2D {
     }
     // CSV layout of save_matrix_to_csv (IO.h:40-69): 15 significant digits, one row per particle,
     // files r_data_<step>.csv, r_data_3D_<step>.csv, particles_color_<step>.csv in ./data.
-    void save_our_data() {
+    void save_our_data(const std::vector<Particle>& ps) {
         std::filesystem::create_directories("data");
-        write_csv("data/r_data_" + std::to_string(current_step_) + ".csv", uv_.data(), 2);
-        write_csv("data/r_data_3D_" + std::to_string(current_step_) + ".csv", r3_.data(), 3);
-        std::ofstream f("data/particles_color_" + std::to_string(current_step_) + ".csv");
-        for (int i = 0; i < n_; ++i) f << cnt_[i] << "\n";
-    }
-    void write_csv(const std::string& path, const double* a, int cols) {
-        std::ofstream f(path);
-        f << std::setprecision(15);
-        for (int i = 0; i < n_; ++i) {
-            for (int c = 0; c < cols; ++c) f << (c ? "," : "") << a[(size_t)i * cols + c];
-            f << "\n";
+        const std::string k = std::to_string(current_step_);
+        std::ofstream uv("data/r_data_" + k + ".csv"), r3("data/r_data_3D_" + k + ".csv");
+        std::ofstream nb("data/particles_color_" + k + ".csv");
+        uv << std::setprecision(15);
+        r3 << std::setprecision(15);
+        for (const Particle& q : ps) {
+            uv << q.x_UV << "," << q.y_UV << "\n";
+            r3 << q.x_3D << "," << q.y_3D << "," << q.z_3D << "\n";
+            nb << q.neighbor_count << "\n";
         }
     }
 
@@ -137,8 +133,6 @@ class Tissue2D {
     int n_, step_count_, current_step_ = 0;
     tds_mesh* mesh_ = nullptr;
     tds_sim* sim_ = nullptr;
-    std::vector<double> uv_, th_, r3_, vel_;
-    std::vector<int> face_, cnt_;
 };
 
 }  // namespace tds

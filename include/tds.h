@@ -129,6 +129,21 @@ int tds_get_state(tds_sim* sim, tds_state_view* out);
  * capture. All calls share the array: calls that overlap on the GPU (other threads or streams)
  * race and must be serialised by the caller; nothing in it needs clearing between calls. */
 int tds_get_state_noalloc(tds_sim* sim, tds_state_view* out);
+/* The reference's per-particle output record (Particle, src/simulation/Struct.h:9-29), same fields,
+ * order and layout (88 bytes): chart position and velocity, the polarity angle in degrees (the
+ * reference stores int degrees), the two compass fields the reference never sets (0), the 3D
+ * position and the neighbour count. */
+typedef struct tds_particle {
+    double x_UV, y_UV;
+    double x_velocity_UV, y_velocity_UV;
+    double alignment_UV;
+    double compass_north_pole_UV, compass_south_pole_UV;
+    double x_3D, y_3D, z_3D;
+    int neighbor_count;
+} tds_particle;
+/* update()'s System.particles (2DTissue.cpp:148-162): the records are packed on the device, in id
+ * order, and copied to out (N records) in one transfer. */
+int tds_get_particles(tds_sim* sim, tds_particle* out);
 /* phi = |sum normalize((r - c) x v)| / N, psi = |sum v/|v|| / N per step and replica:
  * arrays of cap entries, step-major ([step][replica]); *n_steps gets the number of steps stored. */
 int tds_get_order_parameter(tds_sim* sim, double* phi, double* psi, int cap, int* n_steps);

@@ -94,3 +94,24 @@ def test_state_without_r3d_is_the_same_state(tg, mesh_l4, precision):
     sa, sb = a.get_state(), b.get_state()
     for key in sa:
         np.testing.assert_array_equal(sa[key], sb[key])
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_particle_records_match_the_state(tg, mesh_l4, precision):
+    """tds_get_particles packs the reference's Particle records on the device: the same values as
+    the state arrays, the angle in degrees as (theta * 180) / pi, the compass fields 0."""
+    sim = tg.Simulation(mesh_l4, tg.Params(), 700, seed=9, precision=precision)
+    sim.start()
+    sim.step(4)
+    st = sim.get_state()
+    pk = sim.get_particles()
+    assert pk.dtype.itemsize == 88
+    np.testing.assert_array_equal(pk["x_UV"], st["uv"][:, 0])
+    np.testing.assert_array_equal(pk["y_UV"], st["uv"][:, 1])
+    np.testing.assert_array_equal(pk["x_velocity_UV"], st["vel_uv"][:, 0])
+    np.testing.assert_array_equal(pk["y_velocity_UV"], st["vel_uv"][:, 1])
+    np.testing.assert_array_equal(pk["alignment_UV"], st["theta"] * 180.0 / np.pi)
+    np.testing.assert_array_equal(pk["x_3D"], st["r3d"][:, 0])
+    np.testing.assert_array_equal(pk["z_3D"], st["r3d"][:, 2])
+    np.testing.assert_array_equal(pk["neighbor_count"], st["nbr"])
+    assert not pk["compass_north_pole_UV"].any() and not pk["compass_south_pole_UV"].any()
