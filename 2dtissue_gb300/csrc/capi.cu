@@ -458,7 +458,8 @@ template <typename real>
 void flush_finalize(tds_sim* s, const StepHooks* hk = nullptr) {
     {
         KernelTimer kt(s, 4);
-        tdsk::k_finalize<real><<<s->R, 128, 0, s->stream>>>(fin_args<real>(s, hk), s->d_step);
+        tdsk::k_finalize<real><<<(s->R + tdsk::kFinWarps - 1) / tdsk::kFinWarps, 32 * tdsk::kFinWarps, 0, s->stream>>>(
+            fin_args<real>(s, hk), s->d_step);
     }
     cudaMemsetAsync(s->phi_pending, 0, sizeof(int), s->stream);
 }
@@ -479,7 +480,7 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
     int* start = x ? x->start : s->start;
     {
         KernelTimer kt(s, 0);
-        tdsk::k_scan<real><<<s->n_tiles + s->R, tdsk::kScanThreads, 0, st>>>(
+        tdsk::k_scan<real><<<s->n_tiles + (s->R + tdsk::kFinWarps - 1) / tdsk::kFinWarps, tdsk::kScanThreads, 0, st>>>(
             s->count, start, s->M, s->tile_sum, s->n_tiles, s->d_step, fin_args<real>(s, hk));
     }
     const int nb = (s->N + 255) / 256;

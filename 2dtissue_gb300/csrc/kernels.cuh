@@ -50,7 +50,7 @@ enum : int {
 constexpr int kRec = 16;          // reals per face record
 constexpr int kMaxWraps = 8;      // seam wraps per particle per step
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 32;
+constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;  // buckets per scan tile
 constexpr int kStepThreads = 256;  // default block of k_step
 constexpr int kPhiCopies = 32;    // spread the order-parameter atomics over copies
@@ -722,25 +722,31 @@ struct FinArgs {
     int* pending;  // set by k_step, cleared by k_scatter and after a standalone finalize
 };
 
-// One block: replica r's order parameter of `step` into the series; zeroes its accumulators. Warp k
-// sums component k over the kPhiCopies copies in int64 (exact, so the order of the additions does
-// not matter); one conversion to double per component.
+constexpr int kFinWarps = 8;  // replicas finalized per 256-thread block (one warp each)
+static_assert(kScanThreads == 32 * kFinWarps, "k_scan's extra blocks finalize one replica per warp");
+
+// One warp: replica r's order parameter of `step` into the series; zeroes its accumulators. Lane c
+// holds copy c's six components; each component is summed over the kPhiCopies copies in int64
+// (exact, so the order of the additions does not matter), then converted to double once.
 template <typename real>
-__device__ void finalize_replica(const FinArgs<real>& f, int r, long long step, long long* s_v) {
-    const int t = threadIdx.x, lane = t & 31, nw = (int)(blockDim.x >> 5);
+__device__ void finalize_replica(const FinArgs<real>& f, int r, long long step) {
+    const int lane = threadIdx.x & 31;
     static_assert(kPhiCopies == 32, "one copy per lane");
-    for (int k = t >> 5; k < 6; k += nw) {
-        unsigned long long* p = &f.phi_acc[((size_t)r * kPhiCopies + lane) * 6 + k];
-        long long x = (long long)*p;
-        *p = 0ull;
+    unsigned long long* p = &f.phi_acc[((size_t)r * kPhiCopies + lane) * 6];
+    long long x[6];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-        if (lane == 0) s_v[k] = x;
+    for (int k = 0; k < 6; ++k) {
+        x[k] = (long long)p[k];
+        p[k] = 0ull;
     }
-    __syncthreads();
-    if (t == 0) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x[k] += __shfl_xor_sync(0xffffffffu, x[k], o);
+    }
+    if (lane == 0) {
         double v[6];
-        for (int k = 0; k < 6; ++k) v[k] = (double)s_v[k];
+        for (int k = 0; k < 6; ++k) v[k] = (double)x[k];
         const RepParams<real>& rp = f.reps[r];
         const double inv = 1.0 / rp.phiscale;
         const double phi = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) * inv * rp.inv_n;
@@ -770,9 +776,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(int* __restrict__ count, 
     __shared__ int s_warp[kScanThreads / 32];
     __shared__ int s_base;
     if ((int)blockIdx.x >= n_tiles) {
-        __shared__ long long s_fin[6];
         if (*fin.pending == 0) return;
-        finalize_replica(fin, (int)blockIdx.x - n_tiles, *d_step, s_fin);
+        const int r = ((int)blockIdx.x - n_tiles) * kFinWarps + (int)(threadIdx.x >> 5);
+        if (r < fin.R) finalize_replica(fin, r, *d_step);
         return;
     }
     const int tile = blockIdx.x;
@@ -924,9 +930,9 @@ __global__ void __launch_bounds__(kScanThreads) k_tile_sums(const int* __restric
 // runs past its tiles, for a step that no k_scan has followed yet.
 template <typename real>
 __global__ void k_finalize(const FinArgs<real> f, const long long* d_step) {
-    __shared__ long long s[6];
     if (*f.pending == 0) return;
-    finalize_replica(f, (int)blockIdx.x, *d_step, s);
+    const int r = (int)blockIdx.x * kFinWarps + (int)(threadIdx.x >> 5);
+    if (r < f.R) finalize_replica(f, r, *d_step);
 }
 
 // State (physical order) -> id order, in double.
