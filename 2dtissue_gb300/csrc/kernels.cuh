@@ -458,18 +458,21 @@ __device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<re
 }
 
 // Pair sums over a particle's candidate runs in a fixed order (runs 0..8, slots ascending), two
-// candidates per iteration. The run table lives in shared memory, one column per thread (entry r of
-// thread t at srun[r * BLOCK]): switching runs is a shared-memory load instead of a local-memory
-// (L1-cached stack) one, which took the step kernel from 142.7 to 137.0 us at 1M particles.
+// candidates per iteration. The run table lives in shared memory, one column per thread (entry r
+// of thread t at srun[r * BLOCK]): switching runs is a shared-memory load instead of a local-memory
+// (L1-cached stack) one, which took the step kernel from 142.7 to 137.0 us at 1M particles. The
+// table holds the non-empty runs only, so a switch loads the next run once (stepping over empty
+// runs inside the loop cost another 1.5% of the step).
 template <typename real, int BLOCK>
 __device__ __forceinline__ void pair_sums_s(const PairC<real>& pc, const R4<real>& P, const R4<real>* __restrict__ pos,
                                           const R4<real>* __restrict__ pol, const int2* srun, int total, int self,
                                           real (&acc)[6], int& cnt) {
+    if (total == 0) return;
     int r = 0;
     int2 x0 = srun[0];
     int t = x0.x, left = x0.y;
     for (int k = 0; k < total; k += 2) {
-        while (left == 0) {
+        if (left == 0) {
             const int2 x = srun[(++r) * BLOCK];
             t = x.x;
             left = x.y;
@@ -478,7 +481,7 @@ __device__ __forceinline__ void pair_sums_s(const PairC<real>& pc, const R4<real
         --left;
         int tb = -1;
         if (k + 1 < total) {
-            while (left == 0) {
+            if (left == 0) {
                 const int2 x = srun[(++r) * BLOCK];
                 t = x.x;
                 left = x.y;
@@ -522,6 +525,7 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
         // (first slot, count) pairs so that the loop switches runs with one 8-byte load
         __shared__ int2 s_run[9 * BLOCK];
         int2* srun = s_run + threadIdx.x;
+        int nrun = 0;
         int total = 0;
         const int id0 = key0 - rp.base;
         if (id0 < rp.C) {
@@ -534,12 +538,13 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
                 const int b0 = rp.base + first;
                 const int t0 = len ? a.start[b0] : 0;
                 const int t1 = len ? a.start[b0 + len] : 0;
-                srun[r * BLOCK] = make_int2(t0, t1 - t0);
+                // only non-empty runs are kept, in order: the loop never steps over an empty one
+                if (t1 > t0) {
+                    srun[nrun * BLOCK] = make_int2(t0, t1 - t0);
+                    ++nrun;
+                }
                 total += t1 - t0;
             }
-        } else {
-#pragma unroll
-            for (int r = 0; r < 9; ++r) srun[r * BLOCK] = make_int2(0, 0);
         }
         // pair sums over all candidates (in a fixed order); a single-replica system takes the
         // pair constants from the kernel parameters (constant bank) rather than from the replica
