@@ -108,6 +108,7 @@ def lib(build_if_missing=True):
     L.tds_get_state.argtypes = [VP, P(_StateView)]
     L.tds_get_state_noalloc.argtypes = [VP, P(_StateView)]
     L.tds_get_particles.argtypes = [VP, VP]
+    L.tds_step_neighbors.argtypes = [VP, I, VP]
     L.tds_set_state_async.argtypes = [VP, P(_StateView)]
     L.tds_get_state_async.argtypes = [VP, P(_StateView)]
     L.tds_sync.argtypes = [VP]
@@ -376,6 +377,13 @@ class Simulation:
     def adjoint_release(self):
         """Frees the adjoint's work memory that the handle keeps between adjoint() calls."""
         self._check(lib().tds_adjoint_release(self.h))
+
+    def step_neighbors(self, cap=64):
+        """One step that also returns the neighbours it used: (N, cap) int32, row i the indices of
+        particle i's neighbours in the step's visiting order, -1 past the last (test hook)."""
+        out = np.full((self.N, int(cap)), -1, np.int32)
+        self._check(lib().tds_step_neighbors(self.h, int(cap), out.ctypes.data))
+        return out
 
     def get_particles(self):
         """update()'s Particle records (numpy structured array, PARTICLE_DTYPE), packed on the device."""

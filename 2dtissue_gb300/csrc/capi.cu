@@ -466,7 +466,8 @@ void flush_finalize(tds_sim* s, const StepHooks* hk = nullptr) {
 
 // Buffer roles: index 0 = step output (and set_state target), index 1 = sorted copy.
 template <typename real>
-void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullptr) {
+void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullptr, int* nbr_list = nullptr,
+                     int nbr_cap = 0) {
     const int c = 1, o = 0;
     cudaStream_t st = s->stream;
     // the sorted copy and the cell starts of this step go to the handle's buffer 1, or straight
@@ -530,6 +531,8 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
     a.status = s->status;
     a.N = s->N;
     a.single = s->R == 1;
+    a.nbr_list = nbr_list;
+    a.nbr_cap = nbr_cap;
     {
         const RepParams<real>& r0 = *(const RepParams<real>*)s->reps_host.data();
         a.pc0.r_max2 = r0.r_max2, a.pc0.twoR = r0.twoR, a.pc0.inv_twoR = r0.inv_twoR, a.pc0.k = r0.k;
@@ -537,7 +540,9 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
     }
     {
         KernelTimer kt(s, 3);
-        if (s->step_block == 128)
+        if (nbr_list)
+            tdsk::k_step<real, 128, true><<<(s->N + 127) / 128, 128, 0, st>>>(a);
+        else if (s->step_block == 128)
             tdsk::k_step<real, 128><<<(s->N + 127) / 128, 128, 0, st>>>(a);
         else
             tdsk::k_step<real, 256><<<(s->N + 255) / 256, 256, 0, st>>>(a);
@@ -790,6 +795,32 @@ int sync_all(tds_sim* s) {
     }
     return TDS_OK;
 }
+
+// One step that also exports every particle's neighbours (test hook).
+template <typename real>
+int step_neighbors(tds_sim* s, int cap, int* lists) {
+    int rc;
+    if ((rc = sync_all(s))) return rc;
+    if ((rc = ensure_series(s, s->step + 1))) return rc;
+    const long long total = (long long)s->N * cap;
+    int* d = nullptr;
+    if (cudaMalloc(&d, (size_t)total * sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(s, TDS_ERR_NOMEM, "step_neighbors: list allocation");
+    }
+    CK(cudaMemsetAsync(d, 0xFF, (size_t)total * sizeof(int), s->stream));
+    launch_one_step<real>(s, nullptr, nullptr, d, cap);
+    tdsk::k_nbr_ids<real><<<(unsigned)((total + 255) / 256), 256, 0, s->stream>>>(
+        d, cap, s->ids[1], (const RepParams<real>*)s->reps, s->local_bits, total);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(lists, d, (size_t)total * sizeof(int), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(s, TDS_ERR_CUDA, std::string("step_neighbors: ") + cudaGetErrorString(e));
+    s->step += 1;
+    return sync_all(s);
+}
+
 
 // ---------------------------------------------------------------------------------------------
 // Adjoint run (tds_adjoint_run): forward with checkpoints, loss, reverse sweep
@@ -1490,6 +1521,11 @@ int tds_adjoint_release(tds_sim* s) {
 int tds_adjoint_run(tds_sim* s, const tds_adjoint_spec* spec, tds_adjoint_result* out) {
     if (!s || !spec || !out) return TDS_ERR_ARG;
     return s->precision == 32 ? adjoint_run<float>(s, spec, out) : adjoint_run<double>(s, spec, out);
+}
+
+int tds_step_neighbors(tds_sim* s, int cap, int* lists) {
+    if (!s || !lists || cap < 1) return TDS_ERR_ARG;
+    return s->precision == 32 ? step_neighbors<float>(s, cap, lists) : step_neighbors<double>(s, cap, lists);
 }
 
 int tds_get_particles(tds_sim* s, tds_particle* out) {

@@ -123,6 +123,8 @@ struct StepArgs {
     int N;
     int single;  // one replica: pc0 holds its pair constants
     PairC<real> pc0;
+    int* nbr_list;  // neighbour export (the NBR instantiation only): nbr_cap ids per particle
+    int nbr_cap;
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -463,10 +465,11 @@ __device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<re
 // (L1-cached stack) one, which took the step kernel from 142.7 to 137.0 us at 1M particles. The
 // table holds the non-empty runs only, so a switch loads the next run once (stepping over empty
 // runs inside the loop cost another 1.5% of the step).
-template <typename real, int BLOCK>
+// NBR (a test hook's instantiation): each neighbour's sorted slot is also written to list[0..cap).
+template <typename real, int BLOCK, bool NBR = false>
 __device__ __forceinline__ void pair_sums_s(const PairC<real>& pc, const R4<real>& P, const R4<real>* __restrict__ pos,
                                           const R4<real>* __restrict__ pol, const int2* srun, int total, int self,
-                                          real (&acc)[6], int& cnt) {
+                                          real (&acc)[6], int& cnt, int* list = nullptr, int cap = 0) {
     if (total == 0) return;
     int r = 0;
     int2 x0 = srun[0];
@@ -491,15 +494,23 @@ __device__ __forceinline__ void pair_sums_s(const PairC<real>& pc, const R4<real
         }
         const R4<real> Qa = pos[ta];
         const R4<real> Qb = pos[tb >= 0 ? tb : ta];
+        const int c0 = cnt;
         pair_term(pc, P, Qa, pol, ta, ta == self, acc, cnt);
-        if (tb >= 0) pair_term(pc, P, Qb, pol, tb, tb == self, acc, cnt);
+        if (NBR && cnt > c0 && c0 < cap) list[c0] = ta;
+        if (tb >= 0) {
+            const int c1 = cnt;
+            pair_term(pc, P, Qb, pol, tb, tb == self, acc, cnt);
+            if (NBR && cnt > c1 && c1 < cap) list[c1] = tb;
+        }
     }
 }
 
 // BLOCK: threads per block (a tuning choice: 128 or 256); the register budget is the same either
 // way (6 blocks of 256, 12 of 128 per SM in FP32: 40 registers; 6 rather than 5 blocks of 256 took the
 // step from 170.9 to 168.6 us at 1M particles).
-template <typename real, int BLOCK>
+// NBR: the test hook's instantiation that also exports each particle's neighbours (sorted slots,
+// converted to particle indices by k_nbr_ids); the production launches use NBR = false.
+template <typename real, int BLOCK, bool NBR = false>
 __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLOCK) k_step(const StepArgs<real> a) {
     typedef R4<real> r4;
     const int q = blockIdx.x * BLOCK + threadIdx.x;
@@ -551,10 +562,13 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
         // table, so the loop does not re-read them from global memory
         real acc[6] = {0, 0, 0, 0, 0, 0};
         int cnt = 0;
+        int* list = NBR ? a.nbr_list + (size_t)(rp.off + (int)((unsigned)id & ((1u << a.local_bits) - 1u))) * a.nbr_cap
+                        : nullptr;
         if (a.single)
-            pair_sums_s<real, BLOCK>(a.pc0, P, a.pos, a.pol, srun, total, q, acc, cnt);
+            pair_sums_s<real, BLOCK, NBR>(a.pc0, P, a.pos, a.pol, srun, total, q, acc, cnt, list, a.nbr_cap);
         else
-            pair_sums_s<real, BLOCK>(pair_constants(rp), P, a.pos, a.pol, srun, total, q, acc, cnt);
+            pair_sums_s<real, BLOCK, NBR>(pair_constants(rp), P, a.pos, a.pol, srun, total, q, acc, cnt, list,
+                                          a.nbr_cap);
         const real Fxr = acc[0], Fyr = acc[1], Fzr = acc[2];
         const real mxr = acc[3], myr = acc[4], mzr = acc[5];
 
@@ -959,6 +973,19 @@ __global__ void k_gather_state(const R4<real>* pos, const R4<real>* pol, const R
     const R2<real> V = vel[s];
     o_vel[2 * i] = V.x, o_vel[2 * i + 1] = V.y;
     o_cnt[i] = cnt[s];
+}
+
+// Neighbour export (test hook): sorted slots -> particle indices (id order), right after the step
+// that wrote them (its sorted ids are still in place); unused entries stay -1.
+template <typename real>
+__global__ void k_nbr_ids(int* __restrict__ list, int cap, const int* __restrict__ sids,
+                          const RepParams<real>* __restrict__ reps, int local_bits, long long total) {
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= total) return;
+    const int t = list[e];
+    if (t < 0) return;
+    const unsigned id = (unsigned)sids[t];
+    list[e] = reps[id >> local_bits].off + (int)(id & ((1u << local_bits) - 1u));
 }
 
 // State (physical order) -> the reference's Particle records in id order (tds_particle, 88 bytes:

@@ -266,6 +266,12 @@ const char* tds_ref_last_error(const tds_ref_sim* sim);
 void tds_ref_destroy(tds_ref_sim* sim);
 
 /* ---- test hooks ---- */
+/* One step (as tds_step(sim, 1, NULL)) that also returns the neighbours the step used: lists is
+ * N x cap, row i (particle i, id order) holds the indices of its neighbours (j != i, chord distance
+ * below r_max, as the step's pair loop decided) in the step's visiting order, -1 past the last;
+ * a particle with more than cap neighbours keeps the first cap (its count is in nbr_count). The
+ * neighbour sets of the reference's step are its distance matrix rows (Locomotion.cpp:94-138). */
+int tds_step_neighbors(tds_sim* sim, int cap, int* lists);
 /* Runs the device seam wrap (the model form of EuclideanTiling::diagonal_seam_edges_square_border,
  * EuclideanTiling.cpp:31-69) on n points: uv holds the advanced points on entry and the wrapped
  * points on return; theta and vel_uv (2n, may be NULL) are rotated with them. */
