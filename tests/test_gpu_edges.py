@@ -91,3 +91,16 @@ def test_sizes_the_c_abi_rejects(tg, mesh_l4):
     assert e.value.code == 1
     with pytest.raises(tg.TdsError):
         tg.Simulation(mesh_l4, tg.Params(radius=0.05, r_max=0.05), 10)  # r_max must exceed 2R
+
+
+def test_size_limits(tg, mesh_l4):
+    """Beyond the stated maxima the C-ABI answers TDS_ERR_LIMIT before allocating: more than 2^30
+    particles in total, or replica and local indices that do not fit the 31-bit particle id."""
+    with pytest.raises(tg.TdsError) as e:
+        tg.Simulation(mesh_l4, [tg.Params()] * 2, [1 << 30, 1])
+    assert e.value.code == 6
+    ns = [1] * (1 << 17)
+    ns[0] = 1 << 15  # 17 replica bits + 15 local bits > 31
+    with pytest.raises(tg.TdsError) as e:
+        tg.Simulation(mesh_l4, [tg.Params()] * len(ns), ns)
+    assert e.value.code == 6

@@ -152,3 +152,6 @@ def test_ref_step_rejects_bad_input(tg):
     with pytest.raises(tg.TdsError) as e:
         sim.set_state(np.full((10, 2), 0.5), np.zeros(10, np.int32), np.full(10, mesh.Vuv, np.int32))
     assert e.value.code == 1
+    with pytest.raises(tg.TdsError) as e:
+        tg.RefSimulation(mesh, tg.RefParams(), 65537)  # the O(N^2) step's stated maximum
+    assert e.value.code == 6
