@@ -111,6 +111,9 @@ def lib(build_if_missing=True):
     L.tds_step_neighbors.argtypes = [VP, I, VP]
     L.tds_set_state_async.argtypes = [VP, P(_StateView)]
     L.tds_get_state_async.argtypes = [VP, P(_StateView)]
+    # tds_state_view_f32 has the same layout (six pointers)
+    for name in ("tds_set_state_f32", "tds_get_state_f32", "tds_set_state_f32_async", "tds_get_state_f32_async"):
+        getattr(L, name).argtypes = [VP, P(_StateView)]
     L.tds_sync.argtypes = [VP]
     L.tds_set_params.argtypes = [VP, VP]
     L.tds_create_ex.argtypes = [VP, I, VP, VP, C.c_uint64, I, P(_Tuning), P(VP)]
@@ -296,48 +299,57 @@ class Simulation:
         self._check(lib().tds_kernel_times(self.h, ms.ctypes.data, n.ctypes.data))
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(("scan", "scatter", "order", "step", "finalize"))}
 
-    def set_state(self, uv, theta, face=None, r3d=None):
-        uv = np.ascontiguousarray(uv, np.float64)
-        th = np.ascontiguousarray(theta, np.float64)
+    # State transfers. Float arrays are float64 (tds_state_view) or, for an FP32 handle, float32
+    # (tds_state_view_f32: the device values as they are, half the bytes over the host link).
+    def _in_view(self, uv, theta, face, r3d):
+        ft = np.float32 if np.asarray(uv).dtype == np.float32 else np.float64
+        uv = np.ascontiguousarray(uv, ft)
+        th = np.ascontiguousarray(theta, ft)
         fc = None if face is None else np.ascontiguousarray(face, np.int32)
-        r3 = None if r3d is None else np.ascontiguousarray(r3d, np.float64)
-        v = _StateView(_ptr(uv), _ptr(th), _ptr(fc), _ptr(r3), None, None)
-        self._check(lib().tds_set_state(self.h, C.byref(v)))
+        r3 = None if r3d is None else np.ascontiguousarray(r3d, ft)
+        return ft == np.float32, (uv, th, fc, r3), _StateView(_ptr(uv), _ptr(th), _ptr(fc), _ptr(r3), None, None)
 
-    def get_state(self, out=None):
+    def _out_view(self, out, who):
+        fl = [out[k] for k in ("uv", "theta", "r3d", "vel_uv") if out.get(k) is not None]
+        ft = fl[0].dtype if fl else np.dtype(np.float64)
+        if ft not in (np.float32, np.float64):
+            raise ValueError("%s: float arrays must be float64 or float32" % who)
+        for k, dt, per in (("uv", ft, 2), ("theta", ft, 1), ("face", np.int32, 1), ("r3d", ft, 3),
+                           ("vel_uv", ft, 2), ("nbr", np.int32, 1)):
+            a = out.get(k)
+            if a is not None and not (a.flags.c_contiguous and a.dtype == dt and a.size == per * self.N):
+                raise ValueError("%s: out[%r] must be a C-contiguous %s array of %d values"
+                                 % (who, k, np.dtype(dt).name, per * self.N))
+        v = _StateView(_ptr(out.get("uv")), _ptr(out.get("theta")), _ptr(out.get("face")), _ptr(out.get("r3d")),
+                       _ptr(out.get("vel_uv")), _ptr(out.get("nbr")))
+        return ft == np.float32, v
+
+    def set_state(self, uv, theta, face=None, r3d=None):
+        f32, _, v = self._in_view(uv, theta, face, r3d)
+        self._check((lib().tds_set_state_f32 if f32 else lib().tds_set_state)(self.h, C.byref(v)))
+
+    def get_state(self, out=None, dtype=np.float64):
         N = self.N
-        o = out if out is not None else dict(uv=np.zeros((N, 2)), theta=np.zeros(N), face=np.zeros(N, np.int32),
-                                            r3d=np.zeros((N, 3)), vel_uv=np.zeros((N, 2)),
-                                            nbr=np.zeros(N, np.int32))
-        v = _StateView(_ptr(o["uv"]), _ptr(o["theta"]), _ptr(o["face"]), _ptr(o["r3d"]), _ptr(o.get("vel_uv")),
-                       _ptr(o.get("nbr")))
-        self._check(lib().tds_get_state(self.h, C.byref(v)))
+        o = out if out is not None else dict(uv=np.zeros((N, 2), dtype), theta=np.zeros(N, dtype),
+                                            face=np.zeros(N, np.int32), r3d=np.zeros((N, 3), dtype),
+                                            vel_uv=np.zeros((N, 2), dtype), nbr=np.zeros(N, np.int32))
+        f32, v = self._out_view(o, "get_state")
+        self._check((lib().tds_get_state_f32 if f32 else lib().tds_get_state)(self.h, C.byref(v)))
         return o
 
     def set_state_async(self, uv, theta, face=None, r3d=None):
         """Enqueues set_state (upload stream + load on the compute stream) and returns; the
         arrays are held until sync()."""
-        uv = np.ascontiguousarray(uv, np.float64)
-        th = np.ascontiguousarray(theta, np.float64)
-        fc = None if face is None else np.ascontiguousarray(face, np.int32)
-        r3 = None if r3d is None else np.ascontiguousarray(r3d, np.float64)
-        self._pending.append((uv, th, fc, r3))
-        v = _StateView(_ptr(uv), _ptr(th), _ptr(fc), _ptr(r3), None, None)
-        self._check(lib().tds_set_state_async(self.h, C.byref(v)))
+        f32, arrays, v = self._in_view(uv, theta, face, r3d)
+        self._pending.append(arrays)
+        self._check((lib().tds_set_state_f32_async if f32 else lib().tds_set_state_async)(self.h, C.byref(v)))
 
     def get_state_async(self, out):
         """Enqueues get_state into the preallocated arrays of `out` (gather on the compute
         stream, download stream for the copies); they are valid after sync()."""
-        for k, dt, per in (("uv", np.float64, 2), ("theta", np.float64, 1), ("face", np.int32, 1),
-                           ("r3d", np.float64, 3), ("vel_uv", np.float64, 2), ("nbr", np.int32, 1)):
-            a = out.get(k)
-            if a is not None and not (a.flags.c_contiguous and a.dtype == dt and a.size == per * self.N):
-                raise ValueError("get_state_async: out[%r] must be a C-contiguous %s array of %d values"
-                                 % (k, np.dtype(dt).name, per * self.N))
+        f32, v = self._out_view(out, "get_state_async")
         self._pending.append(out)
-        v = _StateView(_ptr(out.get("uv")), _ptr(out.get("theta")), _ptr(out.get("face")), _ptr(out.get("r3d")),
-                       _ptr(out.get("vel_uv")), _ptr(out.get("nbr")))
-        self._check(lib().tds_get_state_async(self.h, C.byref(v)))
+        self._check((lib().tds_get_state_f32_async if f32 else lib().tds_get_state_async)(self.h, C.byref(v)))
 
     def sync(self):
         """Waits for everything enqueued on this handle; raises on a non-zero device status."""

@@ -9,6 +9,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include <nvtx3/nvToolsExt.h>
@@ -635,16 +636,18 @@ struct Carve {
 };
 
 // Loads the state waiting in the input staging (k_load_state computes polarity, cell keys and
-// counts) on the compute stream; per-tile counts for the next scan.
-template <typename real>
+// counts) on the compute stream; per-tile counts for the next scan. I: the staged element type
+// (uv 2N, theta N, r3d 3N values of I at the start of the staging).
+template <typename real, typename I = double>
 int load_from_staging(tds_sim* s, int b, bool has_face, bool has_r3d, bool sync) {
     const size_t N = (size_t)s->N;
     s->cur = 0;
     const int nb = (s->N + 255) / 256;
+    const I* in = reinterpret_cast<const I*>(s->in_d[b]);
     CK(cudaMemsetAsync(s->count, 0, (size_t)s->M * sizeof(int), s->stream));
     CK(cudaMemsetAsync(s->tile_sum, 0, (size_t)2 * s->n_tiles * sizeof(int), s->stream));
-    tdsk::k_load_state<real><<<nb, 256, 0, s->stream>>>(
-        s->in_d[b], s->in_d[b] + 2 * N, s->in_i[b], s->in_d[b] + 3 * N, has_face, has_r3d, (const real*)s->rec, s->adj, s->G,
+    tdsk::k_load_state<real, I><<<nb, 256, 0, s->stream>>>(
+        in, in + 2 * N, s->in_i[b], in + 3 * N, has_face, has_r3d, (const real*)s->rec, s->adj, s->G,
         s->bin_start, s->bin_faces, s->packed_ids, (const RepParams<real>*)s->reps, s->local_bits, s->rows, s->ivals,
         (R4<real>*)s->pos[0], (R4<real>*)s->pol[0], (R2<real>*)s->uv[0], s->ids[0], (R2<real>*)s->vel[0], s->cnt[0],
         s->key[0], s->count, s->N, s->status);
@@ -657,10 +660,12 @@ int load_from_staging(tds_sim* s, int b, bool has_face, bool has_r3d, bool sync)
 }
 
 // Input: host -> input staging on the upload stream, then the load on the compute stream. The
-// upload waits until the previous load has consumed the staging.
-template <typename real>
-int load_state(tds_sim* s, const tds_state_view* in, bool sync) {
+// upload waits until the previous load has consumed the staging. View: tds_state_view (double)
+// or tds_state_view_f32 (float; the staging holds 6N doubles, room for 6N floats).
+template <typename real, typename View>
+int load_state(tds_sim* s, const View* in, bool sync) {
     Range range("tds_set_state");
+    typedef typename std::remove_pointer<decltype(View::uv)>::type I;
     const size_t N = (size_t)s->N;
     if (!in || !in->uv || !in->theta) return fail(s, TDS_ERR_ARG, "set_state needs uv and theta");
     if (in->face) {
@@ -670,18 +675,18 @@ int load_state(tds_sim* s, const tds_state_view* in, bool sync) {
     }
     const int b = s->in_next;
     s->in_next ^= 1;
-    double* d_uv = s->in_d[b];
-    double* d_th = s->in_d[b] + 2 * N;
-    double* d_r3 = s->in_d[b] + 3 * N;
+    I* d_uv = reinterpret_cast<I*>(s->in_d[b]);
+    I* d_th = d_uv + 2 * N;
+    I* d_r3 = d_uv + 3 * N;
     int* d_face = s->in_i[b];
     CK(cudaStreamWaitEvent(s->up, s->ev_in_free[b], 0));
-    CK(cudaMemcpyAsync(d_uv, in->uv, 2 * N * sizeof(double), cudaMemcpyHostToDevice, s->up));
-    CK(cudaMemcpyAsync(d_th, in->theta, N * sizeof(double), cudaMemcpyHostToDevice, s->up));
+    CK(cudaMemcpyAsync(d_uv, in->uv, 2 * N * sizeof(I), cudaMemcpyHostToDevice, s->up));
+    CK(cudaMemcpyAsync(d_th, in->theta, N * sizeof(I), cudaMemcpyHostToDevice, s->up));
     if (in->face) CK(cudaMemcpyAsync(d_face, in->face, N * sizeof(int), cudaMemcpyHostToDevice, s->up));
-    if (in->r3d) CK(cudaMemcpyAsync(d_r3, in->r3d, 3 * N * sizeof(double), cudaMemcpyHostToDevice, s->up));
+    if (in->r3d) CK(cudaMemcpyAsync(d_r3, in->r3d, 3 * N * sizeof(I), cudaMemcpyHostToDevice, s->up));
     CK(cudaEventRecord(s->ev_in_ready[b], s->up));
     CK(cudaStreamWaitEvent(s->stream, s->ev_in_ready[b], 0));
-    return load_from_staging<real>(s, b, in->face != nullptr, in->r3d != nullptr, sync);
+    return load_from_staging<real, I>(s, b, in->face != nullptr, in->r3d != nullptr, sync);
 }
 
 // Places particles on the device (k_place) into the input staging and loads them.
@@ -722,23 +727,26 @@ int start_device(tds_sim* s) {
 }
 
 // Output: gather into the output staging on the compute stream, then device -> host on the
-// download stream. The gather waits until the previous download has left the staging.
-template <typename real>
-int save_state(tds_sim* s, tds_state_view* out, bool sync) {
+// download stream. The gather waits until the previous download has left the staging. View:
+// tds_state_view (double) or tds_state_view_f32 (float; the staging holds 8N doubles, room for
+// 8N floats).
+template <typename real, typename View>
+int save_state(tds_sim* s, View* out, bool sync) {
     Range range("tds_get_state");
+    typedef typename std::remove_pointer<decltype(View::uv)>::type O;
     const size_t N = (size_t)s->N;
     const int b = s->out_next;
     s->out_next ^= 1;
-    double* d_uv = s->st_d[b];
-    double* d_th = s->st_d[b] + 2 * N;
-    double* d_r3 = s->st_d[b] + 3 * N;
-    double* d_vel = s->st_d[b] + 6 * N;
+    O* d_uv = reinterpret_cast<O*>(s->st_d[b]);
+    O* d_th = d_uv + 2 * N;
+    O* d_r3 = d_uv + 3 * N;
+    O* d_vel = d_uv + 6 * N;
     int* d_face = s->st_i[b];
     int* d_cnt = s->st_i[b] + N;
     const int c = s->cur;
     const int nb = (s->N + 255) / 256;
     CK(cudaStreamWaitEvent(s->stream, s->ev_out_free[b], 0));
-    tdsk::k_gather_state<real><<<nb, 256, 0, s->stream>>>(
+    tdsk::k_gather_state<real, O><<<nb, 256, 0, s->stream>>>(
         (const R4<real>*)s->pos[c], (const R4<real>*)s->pol[c], (const R2<real>*)s->uv[c], s->ids[c],
         (const R2<real>*)s->vel[c], s->cnt[c], (const RepParams<real>*)s->reps, s->local_bits, d_uv, d_th, d_face, d_r3,
         d_vel, d_cnt, s->N);
@@ -746,11 +754,11 @@ int save_state(tds_sim* s, tds_state_view* out, bool sync) {
     CK(cudaEventRecord(s->ev_out_ready[b], s->stream));
     CK(cudaStreamWaitEvent(s->down, s->ev_out_ready[b], 0));
     cudaStream_t d = s->down;
-    if (out->uv) CK(cudaMemcpyAsync(out->uv, d_uv, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, d));
-    if (out->theta) CK(cudaMemcpyAsync(out->theta, d_th, N * sizeof(double), cudaMemcpyDeviceToHost, d));
+    if (out->uv) CK(cudaMemcpyAsync(out->uv, d_uv, 2 * N * sizeof(O), cudaMemcpyDeviceToHost, d));
+    if (out->theta) CK(cudaMemcpyAsync(out->theta, d_th, N * sizeof(O), cudaMemcpyDeviceToHost, d));
     if (out->face) CK(cudaMemcpyAsync(out->face, d_face, N * sizeof(int), cudaMemcpyDeviceToHost, d));
-    if (out->r3d) CK(cudaMemcpyAsync(out->r3d, d_r3, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, d));
-    if (out->vel_uv) CK(cudaMemcpyAsync(out->vel_uv, d_vel, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, d));
+    if (out->r3d) CK(cudaMemcpyAsync(out->r3d, d_r3, 3 * N * sizeof(O), cudaMemcpyDeviceToHost, d));
+    if (out->vel_uv) CK(cudaMemcpyAsync(out->vel_uv, d_vel, 2 * N * sizeof(O), cudaMemcpyDeviceToHost, d));
     if (out->nbr_count) CK(cudaMemcpyAsync(out->nbr_count, d_cnt, N * sizeof(int), cudaMemcpyDeviceToHost, d));
     CK(cudaEventRecord(s->ev_out_free[b], d));
     if (sync) CK(cudaStreamSynchronize(d));
@@ -1199,7 +1207,7 @@ int save_state_noalloc(tds_sim* s, tds_state_view* out) {
     int* d_cnt = d_face + N;
     const int c = s->cur;
     const int nb = (s->N + 255) / 256;
-    tdsk::k_gather_state<real><<<nb, 256, 0, s->stream>>>(
+    tdsk::k_gather_state<real, double><<<nb, 256, 0, s->stream>>>(
         (const R4<real>*)s->pos[c], (const R4<real>*)s->pol[c], (const R2<real>*)s->uv[c], s->ids[c],
         (const R2<real>*)s->vel[c], s->cnt[c], (const RepParams<real>*)s->reps, s->local_bits, d_uv, d_th, d_face, d_r3,
         d_vel, d_cnt, s->N);
@@ -1496,6 +1504,33 @@ int tds_set_state_async(tds_sim* s, const tds_state_view* in) {
 int tds_get_state_async(tds_sim* s, tds_state_view* out) {
     if (!s || !out) return TDS_ERR_ARG;
     return s->precision == 32 ? save_state<float>(s, out, false) : save_state<double>(s, out, false);
+}
+
+// The FP32 views: FP32 handles only (an FP64 state would be rounded on the way out).
+static int f32_only(tds_sim* s, const void* view) {
+    if (!s || !view) return TDS_ERR_ARG;
+    if (s->precision != 32) return fail(s, TDS_ERR_ARG, "the FP32 state views need an FP32 handle (precision 32)");
+    return TDS_OK;
+}
+
+int tds_set_state_f32(tds_sim* s, const tds_state_view_f32* in) {
+    if (int rc = f32_only(s, in)) return rc;
+    return load_state<float>(s, in, true);
+}
+
+int tds_get_state_f32(tds_sim* s, tds_state_view_f32* out) {
+    if (int rc = f32_only(s, out)) return rc;
+    return save_state<float>(s, out, true);
+}
+
+int tds_set_state_f32_async(tds_sim* s, const tds_state_view_f32* in) {
+    if (int rc = f32_only(s, in)) return rc;
+    return load_state<float>(s, in, false);
+}
+
+int tds_get_state_f32_async(tds_sim* s, tds_state_view_f32* out) {
+    if (int rc = f32_only(s, out)) return rc;
+    return save_state<float>(s, out, false);
 }
 
 int tds_sync(tds_sim* s) {

@@ -976,12 +976,12 @@ __global__ void k_finalize(const FinArgs<real> f, const long long* d_step) {
     if (r < f.R) finalize_replica(f, r, *d_step);
 }
 
-// State (physical order) -> id order, in double.
-template <typename real>
+// State (physical order) -> id order, in O: double (the reference's type), or float for an FP32
+// state (the values as they are on the device, half the bytes for the host link).
+template <typename real, typename O>
 __global__ void k_gather_state(const R4<real>* pos, const R4<real>* pol, const R2<real>* uv, const int* ids,
                                const R2<real>* vel, const int* cnt, const RepParams<real>* reps, int local_bits,
-                               double* o_uv, double* o_th, int* o_face, double* o_r3d, double* o_vel, int* o_cnt,
-                               int N) {
+                               O* o_uv, O* o_th, int* o_face, O* o_r3d, O* o_vel, int* o_cnt, int N) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= N) return;
     const unsigned id = (unsigned)ids[s];
@@ -1032,11 +1032,12 @@ __global__ void k_pack_particles(const R4<real>* pos, const R2<real>* uv, const 
     out[i] = q;
 }
 
-// Loads a state given in id order (double) into slots = global index; locates faces that are
-// < 0, maps r3d when it is not given, derives the 3D polarity, and counts the particle into its
-// cell bucket for the next step's counting sort (counts must be zero on entry).
-template <typename real>
-__global__ void k_load_state(const double* i_uv, const double* i_th, const int* i_face, const double* i_r3d,
+// Loads a state given in id order (I: double, or float for an FP32 state) into slots = global
+// index; locates faces that are < 0, maps r3d when it is not given, derives the 3D polarity, and
+// counts the particle into its cell bucket for the next step's counting sort (counts must be zero
+// on entry).
+template <typename real, typename I>
+__global__ void k_load_state(const I* i_uv, const I* i_th, const int* i_face, const I* i_r3d,
                              int has_face, int has_r3d, const real* rec, const int4* adj, int G, const int* bs,
                              const int* bf, const int* packed_ids, const RepParams<real>* reps, int local_bits,
                              const int2* rows, const int4* ivals, R4<real>* pos, R4<real>* pol, R2<real>* uv,

@@ -360,49 +360,61 @@ def run_gpu(args):
     # face's chart map of the chart position; tds_set_state derives it on the device when r3d is
     # NULL, bit for bit as the step computes it)
     hin = sim.get_state()
-    pin_in = dict(uv=pinned((n, 2), torch.float64), theta=pinned((n,), torch.float64),
-                  face=pinned((n,), torch.int32))
-    for k in pin_in:
-        pin_in[k][...] = hin[k]
-    pin_out = dict(uv=pinned((n, 2), torch.float64), theta=pinned((n,), torch.float64),
-                   face=pinned((n,), torch.int32), r3d=pinned((n, 3), torch.float64),
-                   vel_uv=pinned((n, 2), torch.float64), nbr=pinned((n,), torch.int32))
-    pin_out2 = {k: pinned(v.shape, torch.float64 if v.dtype == np.float64 else torch.int32) for k, v in pin_out.items()}
     e2e_steps = max(3, min(args.steps, 100))
-    h2d_bytes = int(sum(v.nbytes for v in pin_in.values()))
-    d2h_bytes = int(sum(v.nbytes for v in pin_out.values()))
-    # synchronous: each call returns when its transfer is done
-    sim.set_state(**pin_in)
-    sim.step(1)
-    sim.get_state(pin_out)
-    barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+
+    def end_to_end(fdt):
+        """Per step: state upload, one step, state download, through the state views of float
+        type fdt (torch.float32: tds_*_state_f32*, the FP32 state as it is; torch.float64: the
+        double views). Returns (pipelined s, synchronous s, H2D bytes, D2H bytes)."""
+        pin_in = dict(uv=pinned((n, 2), fdt), theta=pinned((n,), fdt), face=pinned((n,), torch.int32))
+        for k in pin_in:
+            pin_in[k][...] = hin[k]  # FP32 state values: exact in either type
+        out_types = dict(uv=((n, 2), fdt), theta=((n,), fdt), face=((n,), torch.int32), r3d=((n, 3), fdt),
+                         vel_uv=((n, 2), fdt), nbr=((n,), torch.int32))
+        pin_out = {k: pinned(*v) for k, v in out_types.items()}
+        pin_out2 = {k: pinned(*v) for k, v in out_types.items()}
+        h2d = int(sum(v.nbytes for v in pin_in.values()))
+        d2h = int(sum(v.nbytes for v in pin_out.values()))
+        # synchronous: each call returns when its transfer is done
         sim.set_state(**pin_in)
         sim.step(1)
         sim.get_state(pin_out)
-    sync_s = allreduce_max(time.perf_counter() - t0, world)
-    # pipelined: the same calls enqueued; step k+1's upload overlaps step k's download
-    # (host outputs double-buffered, as a caller consuming the results would)
-    sim.set_state_async(**pin_in)
-    sim.step_async(1)
-    sim.get_state_async(pin_out)
-    sim.sync()
-    barrier(world)
-    t0 = time.perf_counter()
-    for k in range(e2e_steps):
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            sim.set_state(**pin_in)
+            sim.step(1)
+            sim.get_state(pin_out)
+        sync_s = allreduce_max(time.perf_counter() - t0, world)
+        # pipelined: the same calls enqueued; step k+1's upload overlaps step k's download
+        # (host outputs double-buffered, as a caller consuming the results would)
         sim.set_state_async(**pin_in)
         sim.step_async(1)
-        sim.get_state_async(pin_out if k % 2 == 0 else pin_out2)
-    sim.sync()
-    e2e_s = allreduce_max(time.perf_counter() - t0, world)
+        sim.get_state_async(pin_out)
+        sim.sync()
+        barrier(world)
+        t0 = time.perf_counter()
+        for k in range(e2e_steps):
+            sim.set_state_async(**pin_in)
+            sim.step_async(1)
+            sim.get_state_async(pin_out if k % 2 == 0 else pin_out2)
+        sim.sync()
+        return allreduce_max(time.perf_counter() - t0, world), sync_s, h2d, d2h
+
+    e2e_s, sync_s, h2d_bytes, d2h_bytes = end_to_end(torch.float32)
+    d_s, d_sync_s, d_h2d, d_d2h = end_to_end(torch.float64)
     e2e = {"value": world * n * e2e_steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
-           "path": "per step: tds_set_state_async of uv, theta, face (pinned H2D, upload stream; r3d derived on "
-                   "the device) + tds_step_async + tds_get_state_async of uv, theta, face, r3d, vel_uv, nbr "
-                   "(pinned D2H, download stream); tds_sync after the last step",
+           "path": "per step: tds_set_state_f32_async of uv, theta, face (pinned H2D, upload stream; r3d derived "
+                   "on the device) + tds_step_async + tds_get_state_f32_async of uv, theta, face, r3d, vel_uv, nbr "
+                   "(pinned D2H, download stream); tds_sync after the last step. The FP32 views carry the FP32 "
+                   "state exactly (the double views return the same values widened)",
            "synchronous": {"value": world * n * e2e_steps / sync_s, "unit": UNIT,
-                           "path": "tds_set_state + tds_step + tds_get_state, each waiting"}}
+                           "path": "tds_set_state_f32 + tds_step + tds_get_state_f32, each waiting"},
+           "double_views": {"value": world * n * e2e_steps / d_s, "unit": UNIT, "h2d_bytes_per_step": d_h2d,
+                            "d2h_bytes_per_step": d_d2h, "synchronous": world * n * e2e_steps / d_sync_s,
+                            "path": "the same loop through tds_set_state_async / tds_get_state_async (double "
+                                    "arrays, the reference's type)"}}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

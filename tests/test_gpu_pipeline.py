@@ -115,3 +115,77 @@ def test_particle_records_match_the_state(tg, mesh_l4, precision):
     np.testing.assert_array_equal(pk["z_3D"], st["r3d"][:, 2])
     np.testing.assert_array_equal(pk["neighbor_count"], st["nbr"])
     assert not pk["compass_north_pole_UV"].any() and not pk["compass_south_pole_UV"].any()
+
+
+def _out32(n):
+    return dict(uv=np.zeros((n, 2), np.float32), theta=np.zeros(n, np.float32), face=np.zeros(n, np.int32),
+                r3d=np.zeros((n, 3), np.float32), vel_uv=np.zeros((n, 2), np.float32), nbr=np.zeros(n, np.int32))
+
+
+def test_fp32_views_are_the_device_state(tg, mesh_l4):
+    """tds_get_state_f32 returns an FP32 handle's state as it is on the device: the double view's
+    values are exactly these, widened. A state set through tds_set_state_f32 is the state set from
+    the same values as doubles, and the steps after it agree bit for bit."""
+    n = 1500
+    (x,) = _inputs(tg, mesh_l4, n, 32, 1)
+    a = tg.Simulation(mesh_l4, tg.Params(), n, seed=4, precision=32)
+    a.set_state(**x)
+    a.step(2)
+    d, f = a.get_state(), a.get_state(dtype=np.float32)
+    for key in ("uv", "theta", "r3d", "vel_uv"):
+        assert f[key].dtype == np.float32
+        np.testing.assert_array_equal(f[key].astype(np.float64), d[key])
+    for key in ("face", "nbr"):
+        np.testing.assert_array_equal(f[key], d[key])
+    b = tg.Simulation(mesh_l4, tg.Params(), n, seed=4, precision=32)
+    c = tg.Simulation(mesh_l4, tg.Params(), n, seed=4, precision=32)
+    b.set_state(f["uv"], f["theta"], f["face"])
+    c.set_state(f["uv"].astype(np.float64), f["theta"].astype(np.float64), f["face"])
+    for _ in range(2):
+        sb, sc = b.get_state(), c.get_state()
+        for key in sb:
+            np.testing.assert_array_equal(sb[key], sc[key])
+        b.step(3)
+        c.step(3)
+
+
+def test_fp32_views_pipelined_match_synchronous(tg, mesh_l4):
+    n = 2000
+    ins = _inputs(tg, mesh_l4, n, 32, 4)
+    ins32 = [dict(uv=x["uv"].astype(np.float32), theta=x["theta"].astype(np.float32), face=x["face"]) for x in ins]
+    ref = tg.Simulation(mesh_l4, tg.Params(), n, seed=3, precision=32)
+    expect = []
+    for x in ins32:
+        ref.set_state(x["uv"].astype(np.float64), x["theta"].astype(np.float64), x["face"])
+        ref.step(1)
+        expect.append(ref.get_state())
+    sim = tg.Simulation(mesh_l4, tg.Params(), n, seed=3, precision=32)
+    outs = [_out32(n) for _ in ins32]
+    for x, o in zip(ins32, outs):
+        sim.set_state_async(**x)
+        sim.step_async(1)
+        sim.get_state_async(o)
+    sim.sync()
+    for e, o in zip(expect, outs):
+        for key in e:
+            np.testing.assert_array_equal(e[key], o[key].astype(e[key].dtype))
+
+
+def test_fp32_views_need_an_fp32_handle(tg, mesh_l4):
+    n = 200
+    sim = tg.Simulation(mesh_l4, tg.Params(), n, seed=1, precision=64)
+    sim.start()
+    with pytest.raises(tg.TdsError) as e:
+        sim.get_state(dtype=np.float32)
+    assert e.value.code == 1
+    with pytest.raises(tg.TdsError) as e:
+        sim.set_state(np.full((n, 2), 0.5, np.float32), np.zeros(n, np.float32))
+    assert e.value.code == 1
+    with pytest.raises(tg.TdsError):
+        sim.get_state_async(_out32(n))
+    # mixed float types in one output set are refused before anything is enqueued
+    o = _out32(n)
+    o["theta"] = np.zeros(n)
+    with pytest.raises(ValueError):
+        sim.get_state_async(o)
+    sim.sync()
