@@ -105,6 +105,7 @@ struct tds_sim {
     double* series = nullptr;
     long long series_cap = 0;  // steps
     int* status = nullptr;
+    int* load_flag = nullptr;  // [0] the load in flight was refused, [1] a refused load not yet reported
     long long* d_step = nullptr;
     int* packed_ids = nullptr;
     void* noise = nullptr;
@@ -332,6 +333,7 @@ int alloc_state(tds_sim* s) {
     if ((rc = dalloc(s, &s->tile_sum, (size_t)2 * s->n_tiles * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->phi_acc, (size_t)s->R * tdsk::kPhiCopies * 6 * sizeof(unsigned long long)))) return rc;
     if ((rc = dalloc(s, &s->status, sizeof(int)))) return rc;
+    if ((rc = dalloc(s, &s->load_flag, 2 * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->phi_pending, sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->d_step, sizeof(long long)))) return rc;
     if ((rc = dalloc(s, &s->packed_ids, N * sizeof(int)))) return rc;
@@ -345,6 +347,7 @@ int alloc_state(tds_sim* s) {
     CK(cudaMemset(s->tile_sum, 0, (size_t)2 * s->n_tiles * sizeof(int)));
     CK(cudaMemset(s->phi_acc, 0, (size_t)s->R * tdsk::kPhiCopies * 6 * sizeof(unsigned long long)));
     CK(cudaMemset(s->status, 0, sizeof(int)));
+    CK(cudaMemset(s->load_flag, 0, 2 * sizeof(int)));
     CK(cudaMemset(s->phi_pending, 0, sizeof(int)));
     const int nN = s->N;
     CK(cudaMemcpy(s->start + s->M, &nN, sizeof(int), cudaMemcpyHostToDevice));
@@ -638,25 +641,43 @@ struct Carve {
 // Loads the state waiting in the input staging (k_load_state computes polarity, cell keys and
 // counts) on the compute stream; per-tile counts for the next scan. I: the staged element type
 // (uv 2N, theta N, r3d 3N values of I at the start of the staging).
+// A load refused on the device (k_check_faces: a face index >= F) is reported once, by the
+// caller's next synchronising call: tds_set_state itself, or tds_sync after tds_set_state_async.
+int take_refused_load(tds_sim* s, const char* who) {
+    int refused = 0;
+    CK(cudaMemcpy(&refused, s->load_flag + 1, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!refused) return TDS_OK;
+    CK(cudaMemset(s->load_flag + 1, 0, sizeof(int)));
+    return fail(s, TDS_ERR_ARG, std::string(who) + ": face index out of range; the load was refused and the "
+                                                   "state is the one before it");
+}
+
+// The face indices are checked on the device (k_check_faces, when check_faces) rather than by a
+// host loop over the caller's array: the host loop took ~0.23 ms of host time per call at 1M
+// particles, about as long as the whole pipelined step. A refused load changes nothing.
 template <typename real, typename I = double>
-int load_from_staging(tds_sim* s, int b, bool has_face, bool has_r3d, bool sync) {
+int load_from_staging(tds_sim* s, int b, bool has_face, bool has_r3d, bool sync, bool check_faces) {
     const size_t N = (size_t)s->N;
     s->cur = 0;
     const int nb = (s->N + 255) / 256;
     const I* in = reinterpret_cast<const I*>(s->in_d[b]);
-    CK(cudaMemsetAsync(s->count, 0, (size_t)s->M * sizeof(int), s->stream));
-    CK(cudaMemsetAsync(s->tile_sum, 0, (size_t)2 * s->n_tiles * sizeof(int), s->stream));
+    CK(cudaMemsetAsync(s->load_flag, 0, sizeof(int), s->stream));
+    if (has_face && check_faces)
+        tdsk::k_check_faces<<<nb, 256, 0, s->stream>>>(s->in_i[b], s->N, s->mesh->t.F, s->load_flag);
+    const int nc = (int)std::min<long long>((s->M + 255) / 256, 8 * 152);
+    tdsk::k_clear_counts<<<nc, 256, 0, s->stream>>>(s->count, s->M, s->tile_sum, 2 * s->n_tiles, s->load_flag);
     tdsk::k_load_state<real, I><<<nb, 256, 0, s->stream>>>(
         in, in + 2 * N, s->in_i[b], in + 3 * N, has_face, has_r3d, (const real*)s->rec, s->adj, s->G,
         s->bin_start, s->bin_faces, s->packed_ids, (const RepParams<real>*)s->reps, s->local_bits, s->rows, s->ivals,
         (R4<real>*)s->pos[0], (R4<real>*)s->pol[0], (R2<real>*)s->uv[0], s->ids[0], (R2<real>*)s->vel[0], s->cnt[0],
-        s->key[0], s->count, s->N, s->status);
+        s->key[0], s->count, s->N, s->status, s->load_flag);
     tdsk::k_tile_sums<<<s->n_tiles, tdsk::kScanThreads, 0, s->stream>>>(s->count, s->M, s->tile_sum, s->n_tiles,
-                                                                         s->d_step);
+                                                                         s->d_step, s->load_flag);
     CK(cudaGetLastError());
     CK(cudaEventRecord(s->ev_in_free[b], s->stream));
-    if (sync) CK(cudaStreamSynchronize(s->stream));
-    return TDS_OK;
+    if (!sync) return TDS_OK;
+    CK(cudaStreamSynchronize(s->stream));
+    return take_refused_load(s, "set_state");
 }
 
 // Input: host -> input staging on the upload stream, then the load on the compute stream. The
@@ -668,11 +689,6 @@ int load_state(tds_sim* s, const View* in, bool sync) {
     typedef typename std::remove_pointer<decltype(View::uv)>::type I;
     const size_t N = (size_t)s->N;
     if (!in || !in->uv || !in->theta) return fail(s, TDS_ERR_ARG, "set_state needs uv and theta");
-    if (in->face) {
-        int fmax = -1;  // branch-free maximum: the compiler vectorises it
-        for (size_t i = 0; i < N; ++i) fmax = std::max(fmax, in->face[i]);
-        if (fmax >= s->mesh->t.F) return fail(s, TDS_ERR_ARG, "set_state: face index out of range");
-    }
     const int b = s->in_next;
     s->in_next ^= 1;
     I* d_uv = reinterpret_cast<I*>(s->in_d[b]);
@@ -686,7 +702,7 @@ int load_state(tds_sim* s, const View* in, bool sync) {
     if (in->r3d) CK(cudaMemcpyAsync(d_r3, in->r3d, 3 * N * sizeof(I), cudaMemcpyHostToDevice, s->up));
     CK(cudaEventRecord(s->ev_in_ready[b], s->up));
     CK(cudaStreamWaitEvent(s->stream, s->ev_in_ready[b], 0));
-    return load_from_staging<real, I>(s, b, in->face != nullptr, in->r3d != nullptr, sync);
+    return load_from_staging<real, I>(s, b, in->face != nullptr, in->r3d != nullptr, sync, true);
 }
 
 // Places particles on the device (k_place) into the input staging and loads them.
@@ -723,7 +739,21 @@ int start_device(tds_sim* s) {
                                                               s->in_d[b], s->in_d[b] + 2 * N, s->in_i[b],
                                                               s->in_d[b] + 3 * N, s->N);
     CK(cudaGetLastError());
-    return load_from_staging<real>(s, b, true, true, true);  // synchronises before the tables are freed
+    // synchronises before the tables are freed; the placed faces are in range by construction
+    return load_from_staging<real>(s, b, true, true, true, false);
+}
+
+// The current state in global index order into o_* (device arrays) on the compute stream; the
+// slot table goes through the handle's perm array.
+template <typename real, typename O>
+void gather_state(tds_sim* s, O* o_uv, O* o_th, int* o_face, O* o_r3d, O* o_vel, int* o_cnt) {
+    const int c = s->cur;
+    const int nb = (s->N + 255) / 256;
+    tdsk::k_slot_of<real><<<nb, 256, 0, s->stream>>>(s->ids[c], (const RepParams<real>*)s->reps, s->local_bits,
+                                                     s->perm, s->N);
+    tdsk::k_gather_state<real, O><<<nb, 256, 0, s->stream>>>(
+        (const R4<real>*)s->pos[c], (const R4<real>*)s->pol[c], (const R2<real>*)s->uv[c], (const R2<real>*)s->vel[c],
+        s->cnt[c], s->perm, o_uv, o_th, o_face, o_r3d, o_vel, o_cnt, s->N);
 }
 
 // Output: gather into the output staging on the compute stream, then device -> host on the
@@ -743,13 +773,8 @@ int save_state(tds_sim* s, View* out, bool sync) {
     O* d_vel = d_uv + 6 * N;
     int* d_face = s->st_i[b];
     int* d_cnt = s->st_i[b] + N;
-    const int c = s->cur;
-    const int nb = (s->N + 255) / 256;
     CK(cudaStreamWaitEvent(s->stream, s->ev_out_free[b], 0));
-    tdsk::k_gather_state<real, O><<<nb, 256, 0, s->stream>>>(
-        (const R4<real>*)s->pos[c], (const R4<real>*)s->pol[c], (const R2<real>*)s->uv[c], s->ids[c],
-        (const R2<real>*)s->vel[c], s->cnt[c], (const RepParams<real>*)s->reps, s->local_bits, d_uv, d_th, d_face, d_r3,
-        d_vel, d_cnt, s->N);
+    gather_state<real, O>(s, d_uv, d_th, d_face, d_r3, d_vel, d_cnt);
     CK(cudaGetLastError());
     CK(cudaEventRecord(s->ev_out_ready[b], s->stream));
     CK(cudaStreamWaitEvent(s->down, s->ev_out_ready[b], 0));
@@ -793,6 +818,7 @@ int sync_all(tds_sim* s) {
     CK(cudaStreamSynchronize(s->up));
     CK(cudaStreamSynchronize(s->stream));
     CK(cudaStreamSynchronize(s->down));
+    if (int rc = take_refused_load(s, "set_state_async")) return rc;
     int st = 0;
     CK(cudaMemcpy(&st, s->status, sizeof(int), cudaMemcpyDeviceToHost));
     if (st) {
@@ -1205,12 +1231,7 @@ int save_state_noalloc(tds_sim* s, tds_state_view* out) {
     double* d_vel = d_uv + 6 * N;
     int* d_face = (int*)(d_uv + 8 * N);
     int* d_cnt = d_face + N;
-    const int c = s->cur;
-    const int nb = (s->N + 255) / 256;
-    tdsk::k_gather_state<real, double><<<nb, 256, 0, s->stream>>>(
-        (const R4<real>*)s->pos[c], (const R4<real>*)s->pol[c], (const R2<real>*)s->uv[c], s->ids[c],
-        (const R2<real>*)s->vel[c], s->cnt[c], (const RepParams<real>*)s->reps, s->local_bits, d_uv, d_th, d_face, d_r3,
-        d_vel, d_cnt, s->N);
+    gather_state<real, double>(s, d_uv, d_th, d_face, d_r3, d_vel, d_cnt);
     CK(cudaGetLastError());
     if (out->uv) CK(cudaMemcpyAsync(out->uv, d_uv, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     if (out->theta) CK(cudaMemcpyAsync(out->theta, d_th, N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));

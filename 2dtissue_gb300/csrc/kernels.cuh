@@ -941,8 +941,9 @@ __global__ void k_order(const int* __restrict__ tmp, const int* __restrict__ key
 // parity the next k_scan reads. Used after a state load, where the counts come from k_load_state.
 __global__ void __launch_bounds__(kScanThreads) k_tile_sums(const int* __restrict__ count, long long M,
                                                             int* __restrict__ tile_sum, int n_tiles,
-                                                            const long long* d_step) {
+                                                            const long long* d_step, const int* flag) {
     __shared__ int s_warp[kScanThreads / 32];
+    if (flag[0]) return;  // a refused load (k_check_faces): the tile counts stay as they were
     const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
     int sum = 0;
     if (base + kScanItems <= M) {
@@ -976,25 +977,40 @@ __global__ void k_finalize(const FinArgs<real> f, const long long* d_step) {
     if (r < f.R) finalize_replica(f, r, *d_step);
 }
 
-// State (physical order) -> id order, in O: double (the reference's type), or float for an FP32
-// state (the values as they are on the device, half the bytes for the host link).
-template <typename real, typename O>
-__global__ void k_gather_state(const R4<real>* pos, const R4<real>* pol, const R2<real>* uv, const int* ids,
-                               const R2<real>* vel, const int* cnt, const RepParams<real>* reps, int local_bits,
-                               O* o_uv, O* o_th, int* o_face, O* o_r3d, O* o_vel, int* o_cnt, int N) {
+// State (physical order) -> id order, in two passes: k_slot_of writes each particle's slot at its
+// global index (one scattered 4-byte store per particle), then k_gather_state reads each
+// particle's records from its slot and writes the outputs in index order, coalesced. (Writing
+// the outputs straight from the slot order scatters six partial-sector stores per particle: the
+// end-to-end loop went 0.335 -> 0.295 ms per step at 1M particles with the two passes.)
+template <typename real>
+__global__ void k_slot_of(const int* __restrict__ ids, const RepParams<real>* __restrict__ reps, int local_bits,
+                          int* __restrict__ slot, int N) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= N) return;
     const unsigned id = (unsigned)ids[s];
-    const int i = reps[id >> local_bits].off + (int)(id & ((1u << local_bits) - 1u));
+    slot[reps[id >> local_bits].off + (int)(id & ((1u << local_bits) - 1u))] = s;
+}
+// O: double (the reference's type), or float for an FP32 state (the values as they are on the
+// device, half the bytes for the host link).
+template <typename real, typename O>
+__global__ void k_gather_state(const R4<real>* __restrict__ pos, const R4<real>* __restrict__ pol,
+                               const R2<real>* __restrict__ uv, const R2<real>* __restrict__ vel,
+                               const int* __restrict__ cnt, const int* __restrict__ slot, O* o_uv, O* o_th,
+                               int* o_face, O* o_r3d, O* o_vel, int* o_cnt, int N) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const int s = slot[i];
     const R4<real> P = pos[s];
     const R2<real> U = uv[s];
+    const R2<real> V = vel[s];
+    const int f = real_to_face(pol[s].w);
+    const int c = cnt[s];
     o_uv[2 * i] = U.x, o_uv[2 * i + 1] = U.y;
     o_th[i] = P.w;
-    o_face[i] = real_to_face(pol[s].w);
+    o_face[i] = f;
     o_r3d[3 * i] = P.x, o_r3d[3 * i + 1] = P.y, o_r3d[3 * i + 2] = P.z;
-    const R2<real> V = vel[s];
     o_vel[2 * i] = V.x, o_vel[2 * i + 1] = V.y;
-    o_cnt[i] = cnt[s];
+    o_cnt[i] = c;
 }
 
 // Neighbour export (test hook): sorted slots -> particle indices (id order), right after the step
@@ -1032,6 +1048,27 @@ __global__ void k_pack_particles(const R4<real>* pos, const R2<real>* uv, const 
     out[i] = q;
 }
 
+// A state load is checked on the device before anything of the current state is touched: a face
+// index >= F refuses the whole load (flag[0], cleared before each load) and records the refusal
+// for the caller (flag[1], sticky until reported); negative indices mean "locate" and are valid.
+// The kernels of the load then leave the state, the cell counts and the tile counts as they were.
+__global__ void k_check_faces(const int* __restrict__ face, int N, int F, int* flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool bad = i < N && face[i] >= F;
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) {
+        atomicOr(&flag[0], 1);
+        atomicOr(&flag[1], 1);
+    }
+}
+// zeroes the cell counts and both parities of the tile counts before a load (unless refused)
+__global__ void k_clear_counts(int* __restrict__ count, long long M, int* __restrict__ tile_sum, int n_tile_sum,
+                               const int* __restrict__ flag) {
+    if (flag[0]) return;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M; i += stride) count[i] = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_tile_sum; i += stride) tile_sum[i] = 0;
+}
+
 // Loads a state given in id order (I: double, or float for an FP32 state) into slots = global
 // index; locates faces that are < 0, maps r3d when it is not given, derives the 3D polarity, and
 // counts the particle into its cell bucket for the next step's counting sort (counts must be zero
@@ -1041,9 +1078,10 @@ __global__ void k_load_state(const I* i_uv, const I* i_th, const int* i_face, co
                              int has_face, int has_r3d, const real* rec, const int4* adj, int G, const int* bs,
                              const int* bf, const int* packed_ids, const RepParams<real>* reps, int local_bits,
                              const int2* rows, const int4* ivals, R4<real>* pos, R4<real>* pol, R2<real>* uv,
-                             int* ids, R2<real>* vel, int* cnt, int* key, int* count, int N, int* status) {
+                             int* ids, R2<real>* vel, int* cnt, int* key, int* count, int N, int* status,
+                             const int* flag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
+    if (i >= N || flag[0]) return;
     const real u = (real)i_uv[2 * i], v = (real)i_uv[2 * i + 1];
     int f = has_face ? i_face[i] : -1;
     if (f < 0) {

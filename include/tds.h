@@ -160,8 +160,10 @@ int tds_step_async(tds_sim* sim, int n_steps);
  * gather and the steps on its compute stream, ordered by events. The host link carries both
  * directions at once, so in a loop set(k) -> step -> get(k) the upload of step k+1 overlaps the
  * download of step k. Host arrays passed in must stay untouched (inputs) or unread (outputs)
- * until tds_sync returns; pinned host memory makes the copies asynchronous. Input validation
- * (face range) happens at the call. */
+ * until tds_sync returns; pinned host memory makes the copies asynchronous. Face indices are
+ * checked on the device: a load with an index >= F is refused as a whole (the state, the cell
+ * lists and everything after it stay as they were) and tds_sync reports it as TDS_ERR_ARG;
+ * tds_set_state reports it itself. Negative indices mean "locate". */
 int tds_set_state_async(tds_sim* sim, const tds_state_view* in);
 int tds_get_state_async(tds_sim* sim, tds_state_view* out);
 /* The state of an FP32 handle in its own precision (no counterpart in the reference, which is

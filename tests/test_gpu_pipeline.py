@@ -50,21 +50,39 @@ def test_pipelined_transfers_match_synchronous(tg, mesh_l4, precision):
         np.testing.assert_array_equal(last[key], outs[-1][key])
 
 
-def test_pipelined_transfer_rejects_bad_faces_before_enqueueing(tg, mesh_l4):
+@pytest.mark.parametrize("use_async", [False, True])
+def test_a_load_with_bad_faces_is_refused_and_changes_nothing(tg, mesh_l4, use_async):
+    """Face indices are checked on the device: a load with an index >= F is refused as a whole,
+    reported by tds_set_state itself or by the next tds_sync, and leaves the state, the cell lists
+    and the steps after it exactly as if the load had not been asked for."""
     n = 500
     (x,) = _inputs(tg, mesh_l4, n, 32, 1)
     sim = tg.Simulation(mesh_l4, tg.Params(), n, seed=1)
+    ref = tg.Simulation(mesh_l4, tg.Params(), n, seed=1)
     sim.set_state(**x)
+    ref.set_state(**x)
     before = sim.get_state()
     bad = dict(x)
     bad["face"] = x["face"].copy()
     bad["face"][7] = mesh_l4.F
-    with pytest.raises(tg.TdsError):
-        sim.set_state_async(**bad)
-    sim.sync()
+    bad["uv"] = x["uv"][::-1].copy()
+    if use_async:
+        sim.set_state_async(**bad)  # enqueued; refused on the device
+        with pytest.raises(tg.TdsError) as e:
+            sim.sync()
+    else:
+        with pytest.raises(tg.TdsError) as e:
+            sim.set_state(**bad)
+    assert e.value.code == 1 and "face index out of range" in str(e.value)
+    sim.sync()  # reported once
     after = sim.get_state()
     for key in before:
         np.testing.assert_array_equal(before[key], after[key])
+    sim.step(3)
+    ref.step(3)
+    a, b = sim.get_state(), ref.get_state()
+    for key in a:
+        np.testing.assert_array_equal(a[key], b[key])
 
 
 def test_get_state_async_checks_output_arrays(tg, mesh_l4):
