@@ -685,6 +685,32 @@ def run_profile(args):
     sim.close()
 
 
+def run_profile_e2e(args):
+    """Minimal driver for ncu: the 1M-particle system, then `steps` iterations of the end-to-end loop
+    (pinned FP32-view upload of uv, theta, face; one step; pinned FP32-view download); no timing."""
+    import torch
+    tg = importlib.import_module("2dtissue_gb300")
+    mesh, p, n = workload_1m(tg)
+    sim = tg.Simulation(mesh, p, n, seed=0, precision=32)
+    sim.start()
+    sim.step(args.warmup)
+    hin = sim.get_state(dtype=np.float32)
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float32 if a.dtype == np.float32 else torch.int32, pin_memory=True)
+        return t.numpy()
+    pin_in = {k: pinned(hin[k]) for k in ("uv", "theta", "face")}
+    for k in pin_in:
+        pin_in[k][...] = hin[k]
+    outs = [{k: pinned(v) for k, v in hin.items()} for _ in range(2)]
+    for k in range(args.steps):
+        sim.set_state_async(**pin_in)
+        sim.step_async(1)
+        sim.get_state_async(outs[k % 2])
+    sim.sync()
+    sim.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -694,6 +720,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", action="store_true", help="only run warmup + steps (for ncu)")
+    ap.add_argument("--e2e", action="store_true", help="with --profile: steps iterations of the end-to-end loop")
     ap.add_argument("--workload", default="plain", choices=["plain", "ensemble", "adjoint", "adjoint_batched", "ref"])
     ap.add_argument("--replicas", type=int, default=4096, help="ensemble workload: replicas")
     ap.add_argument("--sample", type=int, default=256, help="ensemble workload: replicas run one by one")
@@ -702,6 +729,8 @@ def main():
     if args.steps is None:
         args.steps = {"plain": 500, "ensemble": 50, "adjoint": 2000, "adjoint_batched": 500, "ref": 50}[args.workload]
     if args.profile:
+        if args.e2e:
+            return run_profile_e2e(args)
         return run_profile_adjoint(args) if args.workload == "adjoint_batched" else run_profile(args)
     if args.workload == "ensemble" and args.impl != "reference":
         return run_ensemble(args)
