@@ -644,10 +644,13 @@ struct Carve {
 // A load refused on the device (k_check_faces: a face index >= F) is reported once, by the
 // caller's next synchronising call: tds_set_state itself, or tds_sync after tds_set_state_async.
 int take_refused_load(tds_sim* s, const char* who) {
+    // on the handle's (non-blocking) stream, so that the clear is ordered before any later load
     int refused = 0;
-    CK(cudaMemcpy(&refused, s->load_flag + 1, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(&refused, s->load_flag + 1, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
     if (!refused) return TDS_OK;
-    CK(cudaMemset(s->load_flag + 1, 0, sizeof(int)));
+    CK(cudaMemsetAsync(s->load_flag + 1, 0, sizeof(int), s->stream));
+    CK(cudaStreamSynchronize(s->stream));
     return fail(s, TDS_ERR_ARG, std::string(who) + ": face index out of range; the load was refused and the "
                                                    "state is the one before it");
 }
