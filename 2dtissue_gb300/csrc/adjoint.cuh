@@ -65,14 +65,14 @@ struct AdjArgs {
     int N;
 };
 
-// The 9 candidate runs of a particle's cell (slot ranges in the sorted state).
+// The non-empty ones of the 9 candidate runs of a particle's cell (slot ranges in the sorted state),
+// in order, as the step kernel builds them (so pair_sums_s walks them the same way).
 template <typename real>
 __device__ __forceinline__ int candidate_runs(const RepParams<real>& rp, const uint4* desc, const int* start, int key,
                                               int2* run) {
-    int total = 0;
+    int total = 0, nrun = 0;
     const int id0 = key - rp.base;
-#pragma unroll
-    for (int r = 0; r < 9; ++r) run[r * kAdjThreads] = make_int2(0, 0);
+    run[0] = make_int2(0, 0);
     if (id0 < rp.C) {
         const uint4* dp = desc + (size_t)rp.desc_off + (size_t)id0 * 3;
         const uint4 d0 = dp[0], d1 = dp[1], d2 = dp[2];
@@ -83,7 +83,10 @@ __device__ __forceinline__ int candidate_runs(const RepParams<real>& rp, const u
             const int b0 = rp.base + first;
             const int t0 = len ? start[b0] : 0;
             const int t1 = len ? start[b0 + len] : 0;
-            run[r * kAdjThreads] = make_int2(t0, t1 - t0);
+            if (t1 > t0) {
+                run[nrun * kAdjThreads] = make_int2(t0, t1 - t0);
+                ++nrun;
+            }
             total += t1 - t0;
         }
     }
@@ -139,7 +142,8 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 3 : 2)) k_ad
     const int total = candidate_runs(rp, a.desc, a.start, a.key[q], run);
     real acc[6] = {0, 0, 0, 0, 0, 0};
     int cnt = 0;
-    for_candidates(run, total, [&](int t) { pair_term(rp, P, a.pos[t], a.pol, t, t == q, acc, cnt); });
+    // the step kernel's own pair loop (same visiting order and arithmetic: the same sums, bit for bit)
+    pair_sums_s<real, kAdjThreads>(pair_constants(rp), P, a.pos, a.pol, run, total, q, acc, cnt);
     const real p[3] = {PL.x, PL.y, PL.z};
     const real F[3] = {acc[0], acc[1], acc[2]};
     const real m[3] = {acc[3], acc[4], acc[5]};
@@ -328,7 +332,7 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 5 : 3)) k_ad
     for_candidates(run, total, [&](int t) {
         const R4<real> Q = a.pos[t];
         const real dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
-        const real d2 = dx * dx + dy * dy + dz * dz;
+        const real d2 = pair_d2(P, Q);  // the forward's neighbour test, rounded the same way
         if (d2 < rp.r_max2 && t != q) {
             const R4<real> Fj = a.aF[t], Mj = a.aM[t];
             msum[0] += Mj.x, msum[1] += Mj.y, msum[2] += Mj.z;
