@@ -41,7 +41,8 @@ class _Params(C.Structure):
 
 class _AdjSpec(C.Structure):
     _fields_ = [("n_steps", C.c_int), ("checkpoint_stride", C.c_int), ("r3d_target", C.c_void_p),
-                ("w_pos", C.c_double), ("phi_target", C.c_void_p), ("w_phi", C.c_double)]
+                ("w_pos", C.c_double), ("phi_target", C.c_void_p), ("w_phi", C.c_double), ("window", C.c_int),
+                ("reserved", C.c_int)]
 
 
 class _AdjResult(C.Structure):
@@ -370,15 +371,18 @@ class Simulation:
         self._check(lib().tds_set_params(self.h, C.cast(arr, C.c_void_p)))
         self.params = ps
 
-    def adjoint(self, n_steps, r3d_target=None, w_pos=0.0, phi_target=None, w_phi=0.0, checkpoint_stride=0):
+    def adjoint(self, n_steps, r3d_target=None, w_pos=0.0, phi_target=None, w_phi=0.0, checkpoint_stride=0,
+                window=0):
         """Runs n_steps forward from the current state, then the hand-written reverse sweep.
         Loss = w_pos * sum_r mean_i |r_T - r*|^2 + w_phi * sum_t sum_r (phi_t - phi*_t)^2.
         Returns loss, d_params (R x 7, order GRAD_PARAMS), d_uv0 (N x 2), d_theta0 (N) and the
-        checkpoint stride used."""
+        checkpoint stride used. window (0 < window < n_steps): truncated gradient over the last
+        `window` steps; d_uv0 / d_theta0 are then with respect to the state at the window's start."""
         N, R = self.N, self.R
         tgt = None if r3d_target is None else np.ascontiguousarray(r3d_target, np.float64).reshape(N, 3)
         phi = None if phi_target is None else np.ascontiguousarray(phi_target, np.float64).reshape(n_steps, R)
-        spec = _AdjSpec(int(n_steps), int(checkpoint_stride), _ptr(tgt), float(w_pos), _ptr(phi), float(w_phi))
+        spec = _AdjSpec(int(n_steps), int(checkpoint_stride), _ptr(tgt), float(w_pos), _ptr(phi), float(w_phi),
+                        int(window), 0)
         dp = np.zeros((R, 8))
         duv = np.zeros((N, 2))
         dth = np.zeros(N)
@@ -410,8 +414,12 @@ class Simulation:
         o = out if out is not None else dict(uv=np.zeros((N, 2)), theta=np.zeros(N), face=np.zeros(N, np.int32),
                                             r3d=np.zeros((N, 3)), vel_uv=np.zeros((N, 2)),
                                             nbr=np.zeros(N, np.int32))
-        v = _StateView(_ptr(o["uv"]), _ptr(o["theta"]), _ptr(o["face"]), _ptr(o["r3d"]), _ptr(o.get("vel_uv")),
-                       _ptr(o.get("nbr")))
+        # the entry point fills double arrays of N values per component; any array passed is
+        # checked for type, size and layout before the library writes into it (absent keys are
+        # not read back)
+        f32, v = self._out_view(o, "get_state_noalloc")
+        if f32:
+            raise ValueError("get_state_noalloc: float arrays must be float64 (the entry point fills double arrays)")
         self._check(lib().tds_get_state_noalloc(self.h, C.byref(v)))
         return o
 

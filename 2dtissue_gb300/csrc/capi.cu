@@ -938,13 +938,39 @@ struct SegGraphs {
 };
 
 template <typename real>
-int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp, tds_adjoint_result* res) {
+int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* res) {
     Range range("tds_adjoint_run");
-    const int T = sp->n_steps;
-    if (T < 1) return fail(s, TDS_ERR_ARG, "adjoint: n_steps must be >= 1");
-    if (!(sp->w_pos >= 0 && sp->w_phi >= 0)) return fail(s, TDS_ERR_ARG, "adjoint: weights must be >= 0");
+    if (sp_in->n_steps < 1) return fail(s, TDS_ERR_ARG, "adjoint: n_steps must be >= 1");
+    if (!(sp_in->w_pos >= 0 && sp_in->w_phi >= 0)) return fail(s, TDS_ERR_ARG, "adjoint: weights must be >= 0");
+    if (sp_in->window < 0) return fail(s, TDS_ERR_ARG, "adjoint: window must be >= 0");
     int rc;
     if ((rc = sync_all(s))) return rc;
+    // A window shorter than the run: the steps before it run forward only (their order-parameter
+    // terms are added to the loss value), and the reverse sweep covers the window.
+    tds_adjoint_spec spw = *sp_in;
+    double pre_loss = 0.0;
+    if (sp_in->window > 0 && sp_in->window < sp_in->n_steps) {
+        const int pre = sp_in->n_steps - sp_in->window;
+        const long long t_pre = s->step;
+        if ((rc = run_steps<real>(s, pre, nullptr, true))) return rc;
+        if (sp_in->phi_target && sp_in->w_phi > 0) {
+            flush_finalize<real>(s);
+            const size_t R = (size_t)s->R;
+            std::vector<double> ser((size_t)pre * 2 * R);
+            CK(cudaMemcpyAsync(ser.data(), s->series + (size_t)t_pre * 2 * R, ser.size() * sizeof(double),
+                               cudaMemcpyDeviceToHost, s->stream));
+            CK(cudaStreamSynchronize(s->stream));
+            for (int t = 0; t < pre; ++t)
+                for (size_t r = 0; r < R; ++r) {
+                    const double d = ser[(size_t)t * 2 * R + r] - sp_in->phi_target[(size_t)t * R + r];
+                    pre_loss += sp_in->w_phi * d * d;
+                }
+        }
+        spw.n_steps = sp_in->window;
+        spw.phi_target = sp_in->phi_target ? sp_in->phi_target + (size_t)pre * s->R : nullptr;
+    }
+    const tds_adjoint_spec* sp = &spw;
+    const int T = sp->n_steps;
     const size_t N = (size_t)s->N, M = (size_t)s->M, R = (size_t)s->R;
     const size_t b_state = N * (2 * sizeof(R4<real>) + sizeof(R2<real>) + 2 * sizeof(int));
     const size_t b_store = b_state + (M + 1) * sizeof(int);
@@ -1144,7 +1170,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp, tds_adjoint_result* res)
     CK(cudaMemcpyAsync(lh.data(), lam[cur], 3 * N * sizeof(real), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaMemcpyAsync(gh.data(), d_gp, gh.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     if ((rc = sync_all(s))) return rc;
-    res->loss = loss;
+    res->loss = pre_loss + loss;
     res->checkpoint_stride = K;
     if (res->d_params)
         for (size_t i = 0; i < gh.size(); ++i) res->d_params[i] = gh[i];

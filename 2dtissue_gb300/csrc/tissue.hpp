@@ -114,12 +114,14 @@ class Tissue2D {
         if (rc) throw std::runtime_error(std::string("tds: ") + tds_last_error(sim_));
     }
     // CSV layout of save_matrix_to_csv (IO.h:40-69): 15 significant digits, one row per particle,
-    // files r_data_<step>.csv, r_data_3D_<step>.csv, particles_color_<step>.csv in ./data.
+    // files r_data_<step>.csv, r_data_3D_<step>.csv, particles_color_<step>.csv in ./data, opened
+    // in append mode as the reference opens them (IO.h:44), so that a run into a data/ directory
+    // that already holds files of an earlier run adds its rows after theirs.
     void save_our_data(const std::vector<Particle>& ps) {
         std::filesystem::create_directories("data");
         const std::string k = std::to_string(current_step_);
-        std::ofstream uv("data/r_data_" + k + ".csv"), r3("data/r_data_3D_" + k + ".csv");
-        std::ofstream nb("data/particles_color_" + k + ".csv");
+        std::ofstream uv("data/r_data_" + k + ".csv", std::ios::app), r3("data/r_data_3D_" + k + ".csv", std::ios::app);
+        std::ofstream nb("data/particles_color_" + k + ".csv", std::ios::app);
         uv << std::setprecision(15);
         r3 << std::setprecision(15);
         for (const Particle& q : ps) {

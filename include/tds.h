@@ -207,6 +207,16 @@ typedef struct tds_adjoint_spec {
     double w_pos;
     const double* phi_target;  /* n_steps x n_replicas, step-major, or NULL (no order-parameter term) */
     double w_phi;
+    /* 0 (or >= n_steps): the exact gradient of the whole run. 0 < window < n_steps: a truncated
+     * gradient -- the first n_steps - window steps run forward only and the reverse sweep covers
+     * the last `window` steps: d_params sums the parameter sensitivities of those steps (the
+     * order-parameter terms of the earlier steps enter the loss value but not the gradient), and
+     * d_uv0 / d_theta0 are with respect to the state at the window's first step. Over long horizons
+     * the exact gradient of a contact-dominated run grows geometrically with the step count (each
+     * explicit-Euler contact step can multiply a separation error by |1 - 2 dt mu k / 2R|) and
+     * overflows; the window bounds that growth. */
+    int window;
+    int reserved;
 } tds_adjoint_spec;
 typedef struct tds_adjoint_result {
     double loss;

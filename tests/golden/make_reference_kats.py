@@ -6,7 +6,7 @@ Reads (as text) the reference project's tests:
   tests/simulation/test_Locomotion.cpp      (commented out in the reference) repulsive_adhesion (42-60),
                                             mean angle (63-82), symmetrisation (87-136),
                                             get_dist_vect (141-263), average n (279-335)
-Run from the repository root:  python tests/golden/make_reference_kats.py [/path/to/reference]
+Run from the repository root:  python tests/golden/make_reference_kats.py <path to the reference checkout>
 """
 import json
 import math
@@ -14,7 +14,9 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_reference_kats.py <path to the reference checkout>")
+REF = sys.argv[1]
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_kats.json")
 
 

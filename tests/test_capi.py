@@ -48,3 +48,29 @@ def test_null_handles_rejected(tg):
     assert L.tds_step(None, 1, None) == 1
     assert L.tds_get_state(None, None) == 1
     assert L.tds_last_error(None) == b"null handle"
+
+
+def _handle_without_device(tg, n):
+    """A Simulation object with a particle count and no device handle: for the checks that the
+    Python layer makes before it calls the library."""
+    sim = object.__new__(tg.Simulation)
+    sim.N, sim.R, sim.h = n, 1, None
+    return sim
+
+
+@pytest.mark.parametrize("who", ["get_state", "get_state_noalloc"])
+def test_read_back_arrays_are_checked_before_the_call(tg, who):
+    """A float32 array where the entry point writes doubles, a short array or a strided one would
+    be written past its end by the library: they are refused with ValueError before any call."""
+    n = 10
+    sim = _handle_without_device(tg, n)
+    fn = getattr(sim, who)
+    good = dict(uv=np.zeros((n, 2)), theta=np.zeros(n), face=np.zeros(n, np.int32), r3d=np.zeros((n, 3)))
+    for bad in (dict(good, uv=np.zeros((n - 1, 2))), dict(good, theta=np.zeros(2 * n)[::2]),
+                dict(good, face=np.zeros(n, np.int64)), dict(good, r3d=np.zeros((n, 3), np.float32))):
+        with pytest.raises(ValueError):
+            fn(bad)
+    if who == "get_state_noalloc":
+        f32 = {k: (v.astype(np.float32) if v.dtype == np.float64 else v) for k, v in good.items()}
+        with pytest.raises(ValueError):
+            fn(f32)

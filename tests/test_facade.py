@@ -108,3 +108,12 @@ def test_cli_matches_the_python_path(tg, tmp_path):
     np.testing.assert_allclose(r3, st["r3d"], rtol=1e-14, atol=1e-15)
     np.testing.assert_array_equal(nb, st["nbr"])
     assert len(os.listdir(tmp_path / "data")) == 3 * steps
+    # the files are opened in append mode (IO.h:44): a second run into the same directory adds its
+    # rows after the first run's (the same seed gives the same rows)
+    r2 = subprocess.run([CLI, "--step-count", str(steps), "--particle-count", str(n), "--step-time", str(dt),
+                         "--seed", str(seed), "--save-data"], capture_output=True, text=True, cwd=tmp_path)
+    assert r2.returncode == 0, r2.stderr
+    uv2 = np.loadtxt(tmp_path / "data" / ("r_data_%d.csv" % steps), delimiter=",")
+    assert uv2.shape == (2 * n, 2)
+    np.testing.assert_array_equal(uv2[:n], uv)
+    np.testing.assert_array_equal(uv2[n:], uv)

@@ -223,3 +223,32 @@ def test_repeated_adjoint_calls_reuse_the_work_memory(tg, mesh_l4):
             np.testing.assert_array_equal(first[k], o[k])
         # all but eta: dL/d eta weighs the noise draws, which follow the step counter
         np.testing.assert_array_equal(first["d_params"][:, :6], o["d_params"][:, :6])
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_windowed_adjoint_is_the_adjoint_of_its_window(tg, mesh_l4, precision):
+    """window = W < n_steps: the run takes n_steps - W steps forward only, then the adjoint of the
+    last W steps (a truncated gradient). It equals, bit for bit, a plain adjoint of W steps started
+    after the same forward steps; the loss adds the earlier steps' order-parameter terms."""
+    T, W = 10, 4
+    a = _start(tg, mesh_l4, precision, n=400)
+    b = _start(tg, mesh_l4, precision, n=400)
+    s0 = a.get_state()
+    tgt = s0["r3d"] + 0.01
+    phit = np.linspace(0.1, 0.3, T)
+    ra = a.adjoint(T, r3d_target=tgt, w_pos=1.0, phi_target=phit, w_phi=1.0, window=W)
+    b.step(T - W)
+    pre = b.order_parameter()[0][-(T - W):, 0]
+    rb = b.adjoint(W, r3d_target=tgt, w_pos=1.0, phi_target=phit[T - W:], w_phi=1.0)
+    for k in ("d_params", "d_uv0", "d_theta0"):
+        np.testing.assert_array_equal(ra[k], rb[k], err_msg=k)
+    np.testing.assert_allclose(ra["loss"], rb["loss"] + ((pre - phit[:T - W]) ** 2).sum(), rtol=1e-12)
+    sa, sb = a.get_state(), b.get_state()
+    for k in sa:
+        np.testing.assert_array_equal(sa[k], sb[k])
+    # a window covering the whole run is the exact gradient
+    c = _start(tg, mesh_l4, precision, n=400)
+    d = _start(tg, mesh_l4, precision, n=400)
+    rc = c.adjoint(T, r3d_target=tgt, w_pos=1.0, phi_target=phit, w_phi=1.0, window=T)
+    rd = d.adjoint(T, r3d_target=tgt, w_pos=1.0, phi_target=phit, w_phi=1.0)
+    np.testing.assert_array_equal(rc["d_params"], rd["d_params"])

@@ -50,17 +50,26 @@ def test_pipelined_transfers_match_synchronous(tg, mesh_l4, precision):
         np.testing.assert_array_equal(last[key], outs[-1][key])
 
 
+@pytest.mark.parametrize("kind", ["single", "ensemble"])
 @pytest.mark.parametrize("use_async", [False, True])
-def test_a_load_with_bad_faces_is_refused_and_changes_nothing(tg, mesh_l4, use_async):
+def test_a_load_with_bad_faces_is_refused_and_changes_nothing(tg, mesh_l4, use_async, kind):
     """Face indices are checked on the device: a load with an index >= F is refused as a whole,
     reported by tds_set_state itself or by the next tds_sync, and leaves the state, the cell lists
-    and the steps after it exactly as if the load had not been asked for."""
-    n = 500
-    (x,) = _inputs(tg, mesh_l4, n, 32, 1)
-    sim = tg.Simulation(mesh_l4, tg.Params(), n, seed=1)
-    ref = tg.Simulation(mesh_l4, tg.Params(), n, seed=1)
+    and the steps after it exactly as if the load had not been asked for -- on a plain system and
+    on a 3-replica ensemble, after an odd number of steps (the per-tile counts and the step counter
+    have advanced past their initial parity)."""
+    if kind == "single":
+        n, ps = 500, tg.Params()
+    else:
+        n, ps = [200, 137, 163], [tg.Params(eta=0.2), tg.Params(v0=1.3), tg.Params(eta=1.0, v0=0.7)]
+    total = int(np.sum(n))
+    (x,) = _inputs(tg, mesh_l4, total, 32, 1)
+    sim = tg.Simulation(mesh_l4, ps, n, seed=1)
+    ref = tg.Simulation(mesh_l4, ps, n, seed=1)
     sim.set_state(**x)
     ref.set_state(**x)
+    sim.step(3)
+    ref.step(3)
     before = sim.get_state()
     bad = dict(x)
     bad["face"] = x["face"].copy()
@@ -83,6 +92,7 @@ def test_a_load_with_bad_faces_is_refused_and_changes_nothing(tg, mesh_l4, use_a
     a, b = sim.get_state(), ref.get_state()
     for key in a:
         np.testing.assert_array_equal(a[key], b[key])
+    np.testing.assert_array_equal(sim.order_parameter()[0], ref.order_parameter()[0])
 
 
 def test_get_state_async_checks_output_arrays(tg, mesh_l4):
