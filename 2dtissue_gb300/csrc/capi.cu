@@ -125,7 +125,10 @@ struct tds_sim {
     cudaEvent_t ev_out_ready[2] = {nullptr, nullptr}, ev_out_free[2] = {nullptr, nullptr};
     int cur = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    int graph_steps = 16;        // steps per captured CUDA graph (tuning; even)
+    // the whole run as one graph launch: a conditional WHILE node around one step (graph_steps 0)
+    cudaGraphExec_t loop_graph = nullptr;
+    int* loop_left = nullptr;  // device: steps left in the running loop graph
+    int graph_steps = 0;         // 0: loop graph; 2..256 (even): steps per captured chunk (tuning)
     int step_block = 128;        // threads per k_step block (tuning: 128 or 256)
     double cells_per_particle = 4.0;  // cell-level rule (tuning): finest level with C <= max(64, this * N_r)
     double origin[3] = {0, 0, 0};
@@ -139,8 +142,8 @@ struct tds_sim {
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
-    double k_ms[5] = {0, 0, 0, 0, 0};
-    long long k_n[5] = {0, 0, 0, 0, 0};
+    double k_ms[6] = {0, 0, 0, 0, 0, 0};
+    long long k_n[6] = {0, 0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -171,6 +174,10 @@ void free_graphs(tds_sim* s) {
             cudaGraphExecDestroy(g);
             g = nullptr;
         }
+    if (s->loop_graph) {
+        cudaGraphExecDestroy(s->loop_graph);
+        s->loop_graph = nullptr;
+    }
 }
 
 // Model parameters of one replica into its device record (the cell-level fields stay).
@@ -336,6 +343,7 @@ int alloc_state(tds_sim* s) {
     if ((rc = dalloc(s, &s->load_flag, 2 * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->phi_pending, sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->d_step, sizeof(long long)))) return rc;
+    if ((rc = dalloc(s, &s->loop_left, sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->packed_ids, N * sizeof(int)))) return rc;
     for (int b = 0; b < 2; ++b) {
         if ((rc = dalloc(s, &s->st_d[b], 8 * N * sizeof(double)))) return rc;
@@ -510,20 +518,14 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
     a.ids_o = s->ids[o];
     a.vel_o = (R2<real>*)s->vel[o];
     a.cnt_o = s->cnt[o];
-    a.key_o = s->key[o];
     a.key_in = ckey;
     a.desc = s->desc;
     a.start = start;
-    a.count = s->count;
-    a.tile_sum = s->tile_sum;
-    a.n_tiles = s->n_tiles;
     a.rec = (const real*)s->rec;
     a.adj = s->adj;
     a.G = s->G;
     a.bin_start = s->bin_start;
     a.bin_faces = s->bin_faces;
-    a.rows = s->rows;
-    a.ivals = s->ivals;
     a.reps = (const RepParams<real>*)s->reps;
     a.local_bits = s->local_bits;
     a.cx = (real)s->mesh->t.centroid[0], a.cy = (real)s->mesh->t.centroid[1], a.cz = (real)s->mesh->t.centroid[2];
@@ -551,6 +553,47 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
         else
             tdsk::k_step<real, 256><<<(s->N + 255) / 256, 256, 0, st>>>(a);
     }
+    {
+        KernelTimer kt(s, 5);
+        tdsk::k_key<real><<<nb, 256, 0, st>>>((const R4<real>*)s->pos[o], s->ids[o], (const RepParams<real>*)s->reps,
+                                              s->local_bits, s->R == 1, s->rows, s->ivals, s->count, s->key[o],
+                                              s->tile_sum, s->n_tiles, s->d_step, s->status, s->N);
+    }
+}
+
+// The loop graph: a conditional WHILE node whose body (captured from the stream) is one step and
+// k_loop_ctl, which counts the device's step counter down and ends the loop after the last step.
+// One launch runs any number of steps; the step kernels' arguments are the same every step (the
+// step counter, the order-parameter index and the cell lists live on the device).
+template <typename real>
+int build_loop_graph(tds_sim* s) {
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+    if (e == cudaSuccess) {
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(s->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            launch_one_step<real>(s, nullptr);
+            tdsk::k_loop_ctl<<<1, 1, 0, s->stream>>>(s->loop_left, h);
+            e = cudaStreamEndCapture(s->stream, &body);
+        }
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&s->loop_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        s->loop_graph = nullptr;
+        return fail(s, TDS_ERR_CUDA, std::string("loop graph: ") + cudaGetErrorString(e));
+    }
+    return TDS_OK;
 }
 
 template <typename real>
@@ -575,7 +618,16 @@ int run_steps(tds_sim* s, int n, const double* noise_host, bool sync = true) {
         }
     } else {
         int left = n;
-        while (!s->timing && left >= s->graph_steps) {
+        if (!s->timing && s->graph_steps == 0 && left >= 2) {
+            if (!s->loop_graph) {
+                int rc2;
+                if ((rc2 = build_loop_graph<real>(s))) return rc2;
+            }
+            tdsk::k_loop_set<<<1, 1, 0, s->stream>>>(s->loop_left, left);
+            CK(cudaGraphLaunch(s->loop_graph, s->stream));
+            left = 0;
+        }
+        while (!s->timing && s->graph_steps > 0 && left >= s->graph_steps) {
             const int c = s->cur;
             if (!s->graph[c]) {
                 cudaGraph_t g;
@@ -1296,7 +1348,7 @@ int create_impl(const tds_mesh* mesh, int R, const int* n, const tds_params* prm
     s->precision = precision;
     if (tune) {
         if (!(tune->cells_per_particle > 0) || (tune->step_block != 128 && tune->step_block != 256) ||
-            tune->graph_steps < 2 || tune->graph_steps % 2 || tune->graph_steps > 256)
+            (tune->graph_steps != 0 && (tune->graph_steps < 2 || tune->graph_steps % 2 || tune->graph_steps > 256)))
             return TDS_ERR_ARG;
         s->cells_per_particle = tune->cells_per_particle;
         s->step_block = tune->step_block;
@@ -1456,9 +1508,9 @@ int tds_autotune(const tds_mesh* mesh, int n_replicas, const int* n_particles, c
     // caller's workload (created, placed, warmed up, then trial_steps graph-launched steps)
     const double cpp[] = {1.0, 4.0, 16.0};
     const int blocks[] = {128, 256};
-    const int chunks[] = {16, 32};
+    const int chunks[] = {0, 16};  // the loop graph, or graphs of 16 steps
     double best_r = -1;
-    tds_tuning bt{4.0, 256, 16, 0};
+    tds_tuning bt{4.0, 128, 0, 0};
     long long total = 0;
     for (int r = 0; r < n_replicas; ++r) total += n_particles[r];
     for (double c : cpp)
@@ -1470,18 +1522,18 @@ int tds_autotune(const tds_mesh* mesh, int n_replicas, const int* n_particles, c
                 if (rc) return rc;
                 cudaEvent_t e0 = nullptr, e1 = nullptr;
                 float ms = 0;
+                const int steps = g ? (trial_steps + g - 1) / g * g : trial_steps;
                 rc = tds_start(s);
-                if (!rc) rc = tds_step(s, g, nullptr);  // warm-up: graph capture
+                if (!rc) rc = tds_step(s, g ? g : 16, nullptr);  // warm-up: graph capture
                 if (!rc && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
                     cudaEventRecord(e0, s->stream);
-                    rc = tds_step_async(s, (trial_steps + g - 1) / g * g);
+                    rc = tds_step_async(s, steps);
                     cudaEventRecord(e1, s->stream);
                     if (!rc) rc = tds_sync(s);
                     if (!rc) cudaEventElapsedTime(&ms, e0, e1);
                 }
                 if (e0) cudaEventDestroy(e0);
                 if (e1) cudaEventDestroy(e1);
-                const int steps = (trial_steps + g - 1) / g * g;
                 tds_destroy(s);
                 if (rc) return rc;
                 const double rate = ms > 0 ? (double)total * steps / (ms * 1e-3) : 0.0;
@@ -1516,14 +1568,14 @@ int tds_kernel_timing(tds_sim* s, int enable) {
     if (!s) return TDS_ERR_ARG;
     collect_times(s);
     s->timing = enable != 0;
-    for (int k = 0; k < 5; ++k) s->k_ms[k] = 0, s->k_n[k] = 0;
+    for (int k = 0; k < 6; ++k) s->k_ms[k] = 0, s->k_n[k] = 0;
     return TDS_OK;
 }
 
 int tds_kernel_times(tds_sim* s, double* total_ms, long long* launches) {
     if (!s) return TDS_ERR_ARG;
     collect_times(s);
-    for (int k = 0; k < 5; ++k) {
+    for (int k = 0; k < 6; ++k) {
         if (total_ms) total_ms[k] = s->k_ms[k];
         if (launches) launches[k] = s->k_n[k];
     }
@@ -1679,7 +1731,7 @@ int tds_stream(tds_sim* s, void** stream) {
 
 int tds_kernels_per_step(const tds_sim* s, int* n) {
     if (!s || !n) return TDS_ERR_ARG;
-    *n = 4;
+    *n = 5;
     return TDS_OK;
 }
 

@@ -1,6 +1,6 @@
 // sm_103a kernels of the per-step particle update.
 //
-// One step is four launches on the handle's stream (captured in a CUDA graph by the host):
+// One step is five launches on the handle's stream (captured in a CUDA graph by the host):
 //   k_scan     exclusive scan of the cell-list counts; block bases from per-tile counts that the
 //              previous step accumulated (no inter-block waiting); R extra blocks finalize the
 //              previous step's order parameter per replica
@@ -10,7 +10,8 @@
 //              that sorted order: the step kernel reads its own state coalesced and the
 //              candidates of a cell run from consecutive addresses
 //   k_step     fused pair sums + tangent projection + polarity update + chart advance + seam
-//              wrap + face location + chart->3D map + next-step cell key/count + order partials
+//              wrap + face location + chart->3D map + order partials
+//   k_key      next step's cell key of each particle, cell counts and scan-tile counts
 // (k_finalize runs the same per-replica finalize on its own before the series is read.)
 // Replaces (reference): Locomotion::simulate_flight + ForceHelper + OrientationHelper
 // (Locomotion.cpp:57-162, ForceHelper.cpp:34-104, OrientationHelper.cpp:29-116),
@@ -97,20 +98,14 @@ struct StepArgs {
     int* ids_o;
     R2<real>* vel_o;
     int* cnt_o;
-    int* key_o;
     const int* key_in;  // cell bucket of each particle (sorted order)
     const uint4* desc;  // per-cell neighbour-run descriptors, all levels
     const int* start;
-    int* count;
-    int* tile_sum;  // [2][n_tiles]
-    int n_tiles;
     const real* rec;
     const int4* adj;
     int G;
     const int* bin_start;
     const int* bin_faces;
-    const int2* rows;
-    const int4* ivals;
     const RepParams<real>* reps;
     int local_bits;
     real cx, cy, cz;
@@ -536,6 +531,74 @@ __device__ __forceinline__ void pair_sums_s(const PairC<real>& pc, const R4<real
     }
 }
 
+// The same sums in two passes, bit for bit. Pass 1 walks the candidates (runs in order, slots
+// ascending) four at a time: the four slots are taken from the run table, the four positions
+// loaded together, and each candidate that passes the distance test (and is not the particle
+// itself) is appended to the thread's neighbour list in shared memory (one column per thread,
+// kNbCap entries). Pass 2 adds the listed neighbours' terms in list order, two at a time (both
+// neighbours' position and polarity loads in flight together). The list is drained whenever it
+// could overflow, so the terms are added in candidate order, exactly as pair_sums_s adds them.
+// Pass 1 carries no term arithmetic and no polarity loads, so a warp's loop, which runs to its
+// busiest particle's candidate count, issues a fraction of the instructions of the fused loop.
+constexpr int kNbCap = 8;  // neighbour list entries per thread (drained when fewer than 4 are free)
+template <typename real, int BLOCK, bool NBR>
+__device__ __forceinline__ void pair_terms(const PairC<real>& pc, const R4<real>& P, const R4<real>* __restrict__ pos,
+                                           const R4<real>* __restrict__ pol, const int* nb, int k, real (&acc)[6],
+                                           int& cnt, int* list, int cap) {
+    for (int i = 0; i < k; i += 2) {
+        const int ja = nb[i * BLOCK];
+        const bool two = i + 1 < k;
+        const int jb = two ? nb[(i + 1) * BLOCK] : ja;
+        const R4<real> Qa = pos[ja], La = pol[ja];
+        const R4<real> Qb = pos[jb], Lb = pol[jb];
+        if (NBR && cnt < cap) list[cnt] = ja;
+        pair_add(pc, P, Qa, La, acc, cnt);
+        if (two) {
+            if (NBR && cnt < cap) list[cnt] = jb;
+            pair_add(pc, P, Qb, Lb, acc, cnt);
+        }
+    }
+}
+template <typename real, int BLOCK, bool NBR = false>
+__device__ __forceinline__ void pair_sums_2p(const PairC<real>& pc, const R4<real>& P, const R4<real>* __restrict__ pos,
+                                             const R4<real>* __restrict__ pol, const int2* srun, int total, int self,
+                                             real (&acc)[6], int& cnt, int* list = nullptr, int cap = 0) {
+    if (total == 0) return;
+    __shared__ int s_nb[kNbCap * BLOCK];
+    int* nb = s_nb + threadIdx.x;
+    const int2* sp = srun;
+    int2 x0 = *sp;
+    int t = x0.x, left = x0.y;
+    int k = 0;
+    // next candidate slot in visiting order (the table holds non-empty runs only)
+    auto next = [&]() -> int {
+        if (left == 0) {
+            sp += BLOCK;
+            const int2 x = *sp;
+            t = x.x;
+            left = x.y;
+        }
+        --left;
+        return t++;
+    };
+    for (int rem = total; rem > 0; rem -= 4) {
+        if (k > kNbCap - 4) {
+            pair_terms<real, BLOCK, NBR>(pc, P, pos, pol, nb, k, acc, cnt, list, cap);
+            k = 0;
+        }
+        const int j0 = next();
+        const int j1 = rem > 1 ? next() : j0;
+        const int j2 = rem > 2 ? next() : j0;
+        const int j3 = rem > 3 ? next() : j0;
+        const R4<real> Q0 = pos[j0], Q1 = pos[j1], Q2 = pos[j2], Q3 = pos[j3];
+        if (pair_d2(P, Q0) < pc.r_max2 && j0 != self) nb[(k++) * BLOCK] = j0;
+        if (rem > 1 && pair_d2(P, Q1) < pc.r_max2 && j1 != self) nb[(k++) * BLOCK] = j1;
+        if (rem > 2 && pair_d2(P, Q2) < pc.r_max2 && j2 != self) nb[(k++) * BLOCK] = j2;
+        if (rem > 3 && pair_d2(P, Q3) < pc.r_max2 && j3 != self) nb[(k++) * BLOCK] = j3;
+    }
+    pair_terms<real, BLOCK, NBR>(pc, P, pos, pol, nb, k, acc, cnt, list, cap);
+}
+
 // BLOCK: threads per block (a tuning choice: 128 or 256); the register budget is the same either
 // way (6 blocks of 256, 12 of 128 per SM in FP32: 40 registers; 6 rather than 5 blocks of 256 took the
 // step from 170.9 to 168.6 us at 1M particles).
@@ -592,10 +655,10 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
         int* list = NBR ? a.nbr_list + (size_t)(rp.off + (int)((unsigned)id & ((1u << a.local_bits) - 1u))) * a.nbr_cap
                         : nullptr;
         if (a.single)
-            pair_sums_s<real, BLOCK, NBR>(a.pc0, P, a.pos, a.pol, srun, total, q, acc, cnt, list, a.nbr_cap);
+            pair_sums_2p<real, BLOCK, NBR>(a.pc0, P, a.pos, a.pol, srun, total, q, acc, cnt, list, a.nbr_cap);
         else
-            pair_sums_s<real, BLOCK, NBR>(pair_constants(rp), P, a.pos, a.pol, srun, total, q, acc, cnt, list,
-                                          a.nbr_cap);
+            pair_sums_2p<real, BLOCK, NBR>(pair_constants(rp), P, a.pos, a.pol, srun, total, q, acc, cnt, list,
+                                           a.nbr_cap);
         }
         // the rest of the particle's own state, read again (an L1/L2 hit) rather than kept live
         // (spilled at 40 registers) across the pair loop: 64/104 bytes of spill stores/loads per
@@ -692,37 +755,6 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
         r4 ol;
         ol.x = qx, ol.y = qy, ol.z = qz, ol.w = face_to_real(f2, (real)0);
         a.pol_o[q] = ol;
-        // next step's cell key (from the old cell's descriptor when the new cell is one of its 27
-        // neighbours, else by the row lookup), count and scan-tile count (counting sort)
-        int key = -1;
-        {
-            int jx, jy, jz, ix0, iy0, iz0;
-            const r4 P = reload(a.pos, q);
-            const int id0 = reload(a.key_in, q) - rp.base;
-            cell_coords(rp, rx, ry, rz, jx, jy, jz);
-            cell_coords(rp, P.x, P.y, P.z, ix0, iy0, iz0);
-            const int ddy = jy - iy0, ddz = jz - iz0, xo = jx - ix0 + 1;
-            if (ddy >= -1 && ddy <= 1 && ddz >= -1 && ddz <= 1 && xo >= 0 && xo <= 2) {
-                const int r9 = (ddz + 1) * 3 + (ddy + 1);
-                if (id0 < rp.C) {
-                    // the one descriptor word needed, re-read (L1) rather than kept live in
-                    // registers across the pair loop
-                    const unsigned* dw = reinterpret_cast<const unsigned*>(a.desc + (size_t)rp.desc_off + (size_t)id0 * 3);
-                    const unsigned en = dw[r9], gp = dw[9];
-                    const int len = (int)(en & 3u), off = (int)((en >> 2) & 3u), xi = xo - off;
-                    if (!((gp >> r9) & 1u) && xi >= 0 && xi < len) key = rp.base + (int)(en >> 4) + xi;
-                }
-            }
-        }
-        if (key < 0) {
-            bool lost = false;
-            key = bucket_of(rp, a.rows, a.ivals, rx, ry, rz, lost);
-            if (lost) st |= ST_CELL;
-        }
-        atomicAdd(&a.count[key], 1);
-        a.key_o[q] = key;
-        add_tile(a.tile_sum + (size_t)((*a.d_step + 1) & 1) * a.n_tiles, key);
-
         // order-parameter partials: normalize((r' - c) x v), v / |v|
         const real ax = rx - a.cx, ay = ry - a.cy, az = rz - a.cz;
         const real Lx = ay * vz - az * vy, Ly = az * vx - ax * vz, Lz = ax * vy - ay * vx;
@@ -768,6 +800,31 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
             atomicAdd(&a.phi_acc[((size_t)rep * kPhiCopies + copy) * 6 + k],
                       (unsigned long long)__double2ll_rn((double)ph[k] * ps));
     }
+}
+
+// Next step's cell key of every particle: the surface cell of its new position (row table, then the
+// row's x-intervals), counted into the cell counts and its scan tile's count for the counting sort.
+// A position in no surface cell is the reference's lost particle (status bit 16, the particle goes
+// to the replica's overflow bucket). A kernel of its own rather than the tail of k_step: the two
+// dependent table loads per particle are hidden by many resident warps here (few registers),
+// where at the end of the step kernel they were the last links of a long dependent chain.
+template <typename real>
+__global__ void __launch_bounds__(256) k_key(const R4<real>* __restrict__ pos, const int* __restrict__ ids,
+                                             const RepParams<real>* __restrict__ reps, int local_bits, int single,
+                                             const int2* __restrict__ rows, const int4* __restrict__ ivals,
+                                             int* __restrict__ count, int* __restrict__ key_o,
+                                             int* __restrict__ tile_sum, int n_tiles, const long long* d_step,
+                                             int* status, int N) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= N) return;
+    const R4<real> P = pos[q];
+    const int rep = single ? 0 : (int)((unsigned)ids[q] >> local_bits);
+    bool lost = false;
+    const int key = bucket_of(reps[rep], rows, ivals, P.x, P.y, P.z, lost);
+    if (lost) atomicOr(status, ST_CELL);
+    atomicAdd(&count[key], 1);
+    key_o[q] = key;
+    add_tile(tile_sum + (size_t)((*d_step + 1) & 1) * n_tiles, key);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1196,6 +1253,17 @@ __global__ void k_place(const double* __restrict__ frec, const double* __restric
     const double pu3 = ux * p[0] + uy * p[1] + uz * p[2], pv3 = vx * p[0] + vy * p[1] + vz * p[2];
     const double wu = g22 * pu3 - g12 * pv3, wv = g11 * pv3 - g12 * pu3;  // (J^T J)^-1 J^T p times det > 0
     o_th[i] = atan2(wv, wu);
+}
+
+// The run's loop on the device: the handle's loop graph is one conditional WHILE node whose body
+// is one step followed by k_loop_ctl; k_loop_set stores the number of steps before the graph is
+// launched. The body runs while the condition is non-zero: k_loop_ctl counts the steps down and
+// clears the condition after the last one (the host only launches the graph for n >= 1).
+__global__ void k_loop_set(int* left, int n) { *left = n; }
+__global__ void k_loop_ctl(int* left, cudaGraphConditionalHandle h) {
+    const int r = *left - 1;
+    *left = r;
+    cudaGraphSetConditional(h, r > 0 ? 1u : 0u);
 }
 
 template <typename real>

@@ -213,16 +213,29 @@ def test_injected_noise_matches_philox(tg, mesh_l4, orc):
 
 
 def test_graph_and_direct_launches_agree(tg, mesh_l4):
+    """The loop graph (one launch per run, the step count set on the device), graphs of 16 steps
+    and direct launches give the same states and order-parameter series, bit for bit, over runs of
+    different lengths on the same handle."""
+    runs = [37, 2, 3, 16, 1, 25]
     a = tg.Simulation(mesh_l4, tg.Params(), 500, seed=1)
-    a.start()
-    a.step(37)  # 2 graph chunks + 5 direct
+    c = tg.Simulation(mesh_l4, tg.Params(), 500, seed=1,
+                      tuning=dict(cells_per_particle=4.0, step_block=128, graph_steps=16))
+    assert a.tuning()["graph_steps"] == 0
     b = tg.Simulation(mesh_l4, tg.Params(), 500, seed=1)
-    b.start()
-    for _ in range(37):
-        b.step(1)
-    sa, sb = a.get_state(), b.get_state()
-    for k in sa:
-        np.testing.assert_array_equal(sa[k], sb[k])
+    for x in (a, b, c):
+        x.start()
+    for n in runs:
+        a.step(n)  # the loop graph for n >= 2
+        c.step(n)  # chunks of 16 steps + direct launches
+        for _ in range(n):
+            b.step(1)
+        sa, sb, sc = a.get_state(), b.get_state(), c.get_state()
+        for k in sa:
+            np.testing.assert_array_equal(sa[k], sb[k])
+            np.testing.assert_array_equal(sc[k], sb[k])
+    assert a.step_count == b.step_count == sum(runs)
+    np.testing.assert_array_equal(a.order_parameter()[0], b.order_parameter()[0])
+    np.testing.assert_array_equal(c.order_parameter()[0], b.order_parameter()[0])
 
 
 def test_nonfinite_state_reports_status(tg, mesh_l4):

@@ -50,8 +50,8 @@ def test_autotune_returns_a_candidate(tg, mesh_l4):
     ns = [200, 800, 3000]
     t, rate = tg.autotune(mesh_l4, [tg.Params()] * 3, ns, trial_steps=32)
     assert t["cells_per_particle"] in (1.0, 4.0, 16.0) and t["step_block"] in (128, 256)
-    assert t["graph_steps"] in (16, 32) and rate > 0
+    assert t["graph_steps"] in (0, 16) and rate > 0
     sim = tg.Simulation(mesh_l4, [tg.Params()] * 3, ns, tuning=t)
     sim.start()
-    sim.step(t["graph_steps"])
+    sim.step(16)
     assert sim.status() == 0
