@@ -294,12 +294,11 @@ class Simulation:
         self._check(lib().tds_kernel_timing(self.h, int(bool(enable))))
 
     def kernel_times(self):
-        """{name: (total_ms, launches)} for scan, scatter, order, step, finalize, key."""
-        ms = np.zeros(6)
-        n = np.zeros(6, np.int64)
+        """{name: (total_ms, launches)} for scan, scatter, order, step, finalize."""
+        ms = np.zeros(5)
+        n = np.zeros(5, np.int64)
         self._check(lib().tds_kernel_times(self.h, ms.ctypes.data, n.ctypes.data))
-        return {k: (float(ms[i]), int(n[i]))
-                for i, k in enumerate(("scan", "scatter", "order", "step", "finalize", "key"))}
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(("scan", "scatter", "order", "step", "finalize"))}
 
     # State transfers. Float arrays are float64 (tds_state_view) or, for an FP32 handle, float32
     # (tds_state_view_f32: the device values as they are, half the bytes over the host link).

@@ -69,7 +69,7 @@ struct tds_sim {
     std::vector<int> n_rep, off;
     std::vector<tds_params> prm;
     std::vector<int> level_of;  // replica -> cell level
-    int2* rows = nullptr;       // all levels' row tables
+    int4* rows = nullptr;       // all levels' row records (two int4 per grid row)
     int4* ivals = nullptr;      // all levels' x-intervals
     int4* adj = nullptr;        // chart edge adjacency per face
     uint4* desc = nullptr;      // per-cell neighbour-run descriptors (3 uint4 per cell)
@@ -125,9 +125,9 @@ struct tds_sim {
     cudaEvent_t ev_out_ready[2] = {nullptr, nullptr}, ev_out_free[2] = {nullptr, nullptr};
     int cur = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    // the whole run as one graph launch: a conditional WHILE node around one step (graph_steps 0)
+    // the whole run as one graph launch: conditional WHILE nodes around the steps (graph_steps 0)
     cudaGraphExec_t loop_graph = nullptr;
-    int* loop_left = nullptr;  // device: steps left in the running loop graph
+    int* loop_left = nullptr;  // device: [0] step blocks, [1] single steps left in the running loop graph
     int graph_steps = 0;         // 0: loop graph; 2..256 (even): steps per captured chunk (tuning)
     int step_block = 128;        // threads per k_step block (tuning: 128 or 256)
     double cells_per_particle = 4.0;  // cell-level rule (tuning): finest level with C <= max(64, this * N_r)
@@ -142,8 +142,8 @@ struct tds_sim {
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
-    double k_ms[6] = {0, 0, 0, 0, 0, 0};
-    long long k_n[6] = {0, 0, 0, 0, 0, 0};
+    double k_ms[5] = {0, 0, 0, 0, 0};
+    long long k_n[5] = {0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -262,7 +262,7 @@ int upload_tables(tds_sim* s) {
         s->level_of[r] = li;
     }
     std::vector<int> row_off(levels.size()), desc_off(levels.size());
-    std::vector<int2> rows;
+    std::vector<int4> rows;
     std::vector<int4> ivals;
     std::vector<uint32_t> desc;
     for (size_t i = 0; i < levels.size(); ++i) {
@@ -272,16 +272,26 @@ int upload_tables(tds_sim* s) {
         std::vector<uint32_t> d;
         tds::build_cell_descriptors(L, d);
         desc.insert(desc.end(), d.begin(), d.end());
-        row_off[i] = (int)rows.size();
+        row_off[i] = (int)(rows.size() / 2);
         const int ib = (int)ivals.size();
-        for (size_t r = 0; r < L.rows.size() / 2; ++r) rows.push_back(make_int2(L.rows[2 * r] + ib, L.rows[2 * r + 1]));
+        for (size_t r = 0; r < L.rows.size() / 2; ++r) {
+            // the row's first two intervals inline, the rest (if any) in ivals from index first + 2
+            const int first = L.rows[2 * r], n = L.rows[2 * r + 1];
+            int4 a = make_int4(0, -1, 0, n), b = make_int4(0, -1, 0, ib + first);
+            if (n > 0) a = make_int4(L.ivals[4 * first], L.ivals[4 * first + 1], L.ivals[4 * first + 2], n);
+            if (n > 1)
+                b = make_int4(L.ivals[4 * (first + 1)], L.ivals[4 * (first + 1) + 1], L.ivals[4 * (first + 1) + 2],
+                              ib + first);
+            rows.push_back(a);
+            rows.push_back(b);
+        }
         for (size_t v = 0; v < L.ivals.size() / 4; ++v)
             ivals.push_back(make_int4(L.ivals[4 * v], L.ivals[4 * v + 1], L.ivals[4 * v + 2], 0));
     }
     if (ivals.empty()) ivals.push_back(make_int4(0, -1, 0, 0));
-    if ((rc = dalloc(s, &s->rows, rows.size() * sizeof(int2)))) return rc;
+    if ((rc = dalloc(s, &s->rows, rows.size() * sizeof(int4)))) return rc;
     if ((rc = dalloc(s, &s->ivals, ivals.size() * sizeof(int4)))) return rc;
-    CK(cudaMemcpy(s->rows, rows.data(), rows.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->rows, rows.data(), rows.size() * sizeof(int4), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(s->ivals, ivals.data(), ivals.size() * sizeof(int4), cudaMemcpyHostToDevice));
     if (desc.empty()) desc.assign(4, 0u);
     if ((rc = dalloc(s, &s->desc, desc.size() * sizeof(uint32_t)))) return rc;
@@ -343,7 +353,7 @@ int alloc_state(tds_sim* s) {
     if ((rc = dalloc(s, &s->load_flag, 2 * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->phi_pending, sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->d_step, sizeof(long long)))) return rc;
-    if ((rc = dalloc(s, &s->loop_left, sizeof(int)))) return rc;
+    if ((rc = dalloc(s, &s->loop_left, 2 * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->packed_ids, N * sizeof(int)))) return rc;
     for (int b = 0; b < 2; ++b) {
         if ((rc = dalloc(s, &s->st_d[b], 8 * N * sizeof(double)))) return rc;
@@ -518,14 +528,20 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
     a.ids_o = s->ids[o];
     a.vel_o = (R2<real>*)s->vel[o];
     a.cnt_o = s->cnt[o];
+    a.key_o = s->key[o];
     a.key_in = ckey;
     a.desc = s->desc;
     a.start = start;
+    a.count = s->count;
+    a.tile_sum = s->tile_sum;
+    a.n_tiles = s->n_tiles;
     a.rec = (const real*)s->rec;
     a.adj = s->adj;
     a.G = s->G;
     a.bin_start = s->bin_start;
     a.bin_faces = s->bin_faces;
+    a.rows = s->rows;
+    a.ivals = s->ivals;
     a.reps = (const RepParams<real>*)s->reps;
     a.local_bits = s->local_bits;
     a.cx = (real)s->mesh->t.centroid[0], a.cy = (real)s->mesh->t.centroid[1], a.cz = (real)s->mesh->t.centroid[2];
@@ -553,40 +569,53 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
         else
             tdsk::k_step<real, 256><<<(s->N + 255) / 256, 256, 0, st>>>(a);
     }
-    {
-        KernelTimer kt(s, 5);
-        tdsk::k_key<real><<<nb, 256, 0, st>>>((const R4<real>*)s->pos[o], s->ids[o], (const RepParams<real>*)s->reps,
-                                              s->local_bits, s->R == 1, s->rows, s->ivals, s->count, s->key[o],
-                                              s->tile_sum, s->n_tiles, s->d_step, s->status, s->N);
-    }
 }
 
-// The loop graph: a conditional WHILE node whose body (captured from the stream) is one step and
-// k_loop_ctl, which counts the device's step counter down and ends the loop after the last step.
-// One launch runs any number of steps; the step kernels' arguments are the same every step (the
-// step counter, the order-parameter index and the cell lists live on the device).
+// The loop graph: k_loop_arm, then a conditional WHILE node whose body (captured from the stream)
+// is kLoopBlock steps and k_loop_ctl, then one whose body is a single step and k_loop_ctl. A run of n
+// steps stores n / kLoopBlock and n % kLoopBlock on the device (k_loop_set) and launches the graph
+// once; the step kernels' arguments are the same every step (the step counter, the order-parameter
+// index and the cell lists live on the device). The block body keeps the per-pass cost of the loop
+// (a conditional re-launch of the body) off every step of a small system.
+constexpr int kLoopBlock = 16;
+
 template <typename real>
 int build_loop_graph(tds_sim* s) {
     cudaGraph_t g = nullptr;
     CK(cudaGraphCreate(&g, 0));
-    cudaGraphConditionalHandle h;
-    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
-    cudaGraphNodeParams np = {};
-    np.type = cudaGraphNodeTypeConditional;
-    np.conditional.handle = h;
-    np.conditional.type = cudaGraphCondTypeWhile;
-    np.conditional.size = 1;
-    cudaGraphNode_t node;
-    if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+    cudaGraphConditionalHandle hb = 0, h1 = 0;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&hb, g, 0, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h1, g, 0, cudaGraphCondAssignDefault);
+    cudaGraphNode_t arm = nullptr, nb = nullptr, n1 = nullptr;
     if (e == cudaSuccess) {
-        cudaGraph_t body = np.conditional.phGraph_out[0];
-        e = cudaStreamBeginCaptureToGraph(s->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            launch_one_step<real>(s, nullptr);
-            tdsk::k_loop_ctl<<<1, 1, 0, s->stream>>>(s->loop_left, h);
-            e = cudaStreamEndCapture(s->stream, &body);
-        }
+        int* left = s->loop_left;
+        void* args[] = {&left, &hb, &h1};
+        cudaKernelNodeParams kp = {};
+        kp.func = (void*)tdsk::k_loop_arm;
+        kp.gridDim = dim3(1);
+        kp.blockDim = dim3(1);
+        kp.kernelParams = args;
+        e = cudaGraphAddKernelNode(&arm, g, nullptr, 0, &kp);
     }
+    // one WHILE node after `dep` whose body is `steps` steps and the count-down of left[which]
+    auto add_loop = [&](cudaGraphNode_t dep, cudaGraphConditionalHandle h, int steps, int which,
+                        cudaGraphNode_t* out) -> cudaError_t {
+        cudaGraphNodeParams np = {};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaError_t r = cudaGraphAddNode(out, g, &dep, nullptr, 1, &np);
+        if (r != cudaSuccess) return r;
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        r = cudaStreamBeginCaptureToGraph(s->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (r != cudaSuccess) return r;
+        for (int k = 0; k < steps; ++k) launch_one_step<real>(s, nullptr);
+        tdsk::k_loop_ctl<<<1, 1, 0, s->stream>>>(s->loop_left + which, h);
+        return cudaStreamEndCapture(s->stream, &body);
+    };
+    if (e == cudaSuccess) e = add_loop(arm, hb, kLoopBlock, 0, &nb);
+    if (e == cudaSuccess) e = add_loop(nb, h1, 1, 1, &n1);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&s->loop_graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) {
@@ -623,7 +652,7 @@ int run_steps(tds_sim* s, int n, const double* noise_host, bool sync = true) {
                 int rc2;
                 if ((rc2 = build_loop_graph<real>(s))) return rc2;
             }
-            tdsk::k_loop_set<<<1, 1, 0, s->stream>>>(s->loop_left, left);
+            tdsk::k_loop_set<<<1, 1, 0, s->stream>>>(s->loop_left, left / kLoopBlock, left % kLoopBlock);
             CK(cudaGraphLaunch(s->loop_graph, s->stream));
             left = 0;
         }
@@ -1568,14 +1597,14 @@ int tds_kernel_timing(tds_sim* s, int enable) {
     if (!s) return TDS_ERR_ARG;
     collect_times(s);
     s->timing = enable != 0;
-    for (int k = 0; k < 6; ++k) s->k_ms[k] = 0, s->k_n[k] = 0;
+    for (int k = 0; k < 5; ++k) s->k_ms[k] = 0, s->k_n[k] = 0;
     return TDS_OK;
 }
 
 int tds_kernel_times(tds_sim* s, double* total_ms, long long* launches) {
     if (!s) return TDS_ERR_ARG;
     collect_times(s);
-    for (int k = 0; k < 6; ++k) {
+    for (int k = 0; k < 5; ++k) {
         if (total_ms) total_ms[k] = s->k_ms[k];
         if (launches) launches[k] = s->k_n[k];
     }
@@ -1731,7 +1760,7 @@ int tds_stream(tds_sim* s, void** stream) {
 
 int tds_kernels_per_step(const tds_sim* s, int* n) {
     if (!s || !n) return TDS_ERR_ARG;
-    *n = 5;
+    *n = 4;
     return TDS_OK;
 }
 

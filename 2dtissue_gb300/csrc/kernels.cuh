@@ -1,6 +1,6 @@
 // sm_103a kernels of the per-step particle update.
 //
-// One step is five launches on the handle's stream (captured in a CUDA graph by the host):
+// One step is four launches on the handle's stream (captured in a CUDA graph by the host):
 //   k_scan     exclusive scan of the cell-list counts; block bases from per-tile counts that the
 //              previous step accumulated (no inter-block waiting); R extra blocks finalize the
 //              previous step's order parameter per replica
@@ -10,8 +10,7 @@
 //              that sorted order: the step kernel reads its own state coalesced and the
 //              candidates of a cell run from consecutive addresses
 //   k_step     fused pair sums + tangent projection + polarity update + chart advance + seam
-//              wrap + face location + chart->3D map + order partials
-//   k_key      next step's cell key of each particle, cell counts and scan-tile counts
+//              wrap + face location + chart->3D map + next-step cell key/count + order partials
 // (k_finalize runs the same per-replica finalize on its own before the series is read.)
 // Replaces (reference): Locomotion::simulate_flight + ForceHelper + OrientationHelper
 // (Locomotion.cpp:57-162, ForceHelper.cpp:34-104, OrientationHelper.cpp:29-116),
@@ -98,14 +97,20 @@ struct StepArgs {
     int* ids_o;
     R2<real>* vel_o;
     int* cnt_o;
+    int* key_o;
     const int* key_in;  // cell bucket of each particle (sorted order)
     const uint4* desc;  // per-cell neighbour-run descriptors, all levels
     const int* start;
+    int* count;
+    int* tile_sum;  // [2][n_tiles]
+    int n_tiles;
     const real* rec;
     const int4* adj;
     int G;
     const int* bin_start;
     const int* bin_faces;
+    const int4* rows;  // row records (two int4 per grid row, see bucket_of)
+    const int4* ivals;
     const RepParams<real>* reps;
     int local_bits;
     real cx, cy, cz;
@@ -378,19 +383,24 @@ __device__ __forceinline__ void cell_coords(const RepParams<real>& rp, real x, r
     iy = min(max((int)d_floor((y - rp.oy) * rp.inv_h), 1), rp.gy - 2);
     iz = min(max((int)d_floor((z - rp.oz) * rp.inv_h), 1), rp.gz - 2);
 }
-// bucket of a position: base + surface-cell id, or base + C when the cell is not a surface cell
+// bucket of a position: base + surface-cell id, or base + C when the cell is not a surface cell.
+// Row records are two int4 per grid row (iz, iy): {x_lo, x_hi, first id, intervals} and the same for
+// the second interval with the index of the row's intervals in `ivals` in place of the count. A row
+// crosses the surface in at most two x-intervals on a convex or mildly bumpy surface, so the lookup
+// is one 32-byte load; rows with more intervals continue in `ivals`.
 template <typename real>
-__device__ __forceinline__ int bucket_of(const RepParams<real>& rp, const int2* rows, const int4* ivals, real x,
+__device__ __forceinline__ int bucket_of(const RepParams<real>& rp, const int4* rows, const int4* ivals, real x,
                                          real y, real z, bool& lost) {
     int ix, iy, iz;
     cell_coords(rp, x, y, z, ix, iy, iz);
-    const int2 R = rows[rp.row_off + iz * rp.gy + iy];
-    for (int k = 0; k < R.y; ++k) {
-        const int4 I = ivals[R.x + k];
-        if (ix >= I.x && ix <= I.y) {
-            lost = false;
-            return rp.base + I.z + ix - I.x;
-        }
+    const int4* R = rows + 2 * (size_t)(rp.row_off + iz * rp.gy + iy);
+    const int4 A = R[0], B = R[1];
+    lost = false;
+    if (A.w > 0 && ix >= A.x && ix <= A.y) return rp.base + A.z + ix - A.x;
+    if (A.w > 1 && ix >= B.x && ix <= B.y) return rp.base + B.z + ix - B.x;
+    for (int k = 2; k < A.w; ++k) {
+        const int4 I = ivals[B.w + k];
+        if (ix >= I.x && ix <= I.y) return rp.base + I.z + ix - I.x;
     }
     lost = true;
     return rp.base + rp.C;
@@ -531,74 +541,6 @@ __device__ __forceinline__ void pair_sums_s(const PairC<real>& pc, const R4<real
     }
 }
 
-// The same sums in two passes, bit for bit. Pass 1 walks the candidates (runs in order, slots
-// ascending) four at a time: the four slots are taken from the run table, the four positions
-// loaded together, and each candidate that passes the distance test (and is not the particle
-// itself) is appended to the thread's neighbour list in shared memory (one column per thread,
-// kNbCap entries). Pass 2 adds the listed neighbours' terms in list order, two at a time (both
-// neighbours' position and polarity loads in flight together). The list is drained whenever it
-// could overflow, so the terms are added in candidate order, exactly as pair_sums_s adds them.
-// Pass 1 carries no term arithmetic and no polarity loads, so a warp's loop, which runs to its
-// busiest particle's candidate count, issues a fraction of the instructions of the fused loop.
-constexpr int kNbCap = 8;  // neighbour list entries per thread (drained when fewer than 4 are free)
-template <typename real, int BLOCK, bool NBR>
-__device__ __forceinline__ void pair_terms(const PairC<real>& pc, const R4<real>& P, const R4<real>* __restrict__ pos,
-                                           const R4<real>* __restrict__ pol, const int* nb, int k, real (&acc)[6],
-                                           int& cnt, int* list, int cap) {
-    for (int i = 0; i < k; i += 2) {
-        const int ja = nb[i * BLOCK];
-        const bool two = i + 1 < k;
-        const int jb = two ? nb[(i + 1) * BLOCK] : ja;
-        const R4<real> Qa = pos[ja], La = pol[ja];
-        const R4<real> Qb = pos[jb], Lb = pol[jb];
-        if (NBR && cnt < cap) list[cnt] = ja;
-        pair_add(pc, P, Qa, La, acc, cnt);
-        if (two) {
-            if (NBR && cnt < cap) list[cnt] = jb;
-            pair_add(pc, P, Qb, Lb, acc, cnt);
-        }
-    }
-}
-template <typename real, int BLOCK, bool NBR = false>
-__device__ __forceinline__ void pair_sums_2p(const PairC<real>& pc, const R4<real>& P, const R4<real>* __restrict__ pos,
-                                             const R4<real>* __restrict__ pol, const int2* srun, int total, int self,
-                                             real (&acc)[6], int& cnt, int* list = nullptr, int cap = 0) {
-    if (total == 0) return;
-    __shared__ int s_nb[kNbCap * BLOCK];
-    int* nb = s_nb + threadIdx.x;
-    const int2* sp = srun;
-    int2 x0 = *sp;
-    int t = x0.x, left = x0.y;
-    int k = 0;
-    // next candidate slot in visiting order (the table holds non-empty runs only)
-    auto next = [&]() -> int {
-        if (left == 0) {
-            sp += BLOCK;
-            const int2 x = *sp;
-            t = x.x;
-            left = x.y;
-        }
-        --left;
-        return t++;
-    };
-    for (int rem = total; rem > 0; rem -= 4) {
-        if (k > kNbCap - 4) {
-            pair_terms<real, BLOCK, NBR>(pc, P, pos, pol, nb, k, acc, cnt, list, cap);
-            k = 0;
-        }
-        const int j0 = next();
-        const int j1 = rem > 1 ? next() : j0;
-        const int j2 = rem > 2 ? next() : j0;
-        const int j3 = rem > 3 ? next() : j0;
-        const R4<real> Q0 = pos[j0], Q1 = pos[j1], Q2 = pos[j2], Q3 = pos[j3];
-        if (pair_d2(P, Q0) < pc.r_max2 && j0 != self) nb[(k++) * BLOCK] = j0;
-        if (rem > 1 && pair_d2(P, Q1) < pc.r_max2 && j1 != self) nb[(k++) * BLOCK] = j1;
-        if (rem > 2 && pair_d2(P, Q2) < pc.r_max2 && j2 != self) nb[(k++) * BLOCK] = j2;
-        if (rem > 3 && pair_d2(P, Q3) < pc.r_max2 && j3 != self) nb[(k++) * BLOCK] = j3;
-    }
-    pair_terms<real, BLOCK, NBR>(pc, P, pos, pol, nb, k, acc, cnt, list, cap);
-}
-
 // BLOCK: threads per block (a tuning choice: 128 or 256); the register budget is the same either
 // way (6 blocks of 256, 12 of 128 per SM in FP32: 40 registers; 6 rather than 5 blocks of 256 took the
 // step from 170.9 to 168.6 us at 1M particles).
@@ -655,10 +597,10 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
         int* list = NBR ? a.nbr_list + (size_t)(rp.off + (int)((unsigned)id & ((1u << a.local_bits) - 1u))) * a.nbr_cap
                         : nullptr;
         if (a.single)
-            pair_sums_2p<real, BLOCK, NBR>(a.pc0, P, a.pos, a.pol, srun, total, q, acc, cnt, list, a.nbr_cap);
+            pair_sums_s<real, BLOCK, NBR>(a.pc0, P, a.pos, a.pol, srun, total, q, acc, cnt, list, a.nbr_cap);
         else
-            pair_sums_2p<real, BLOCK, NBR>(pair_constants(rp), P, a.pos, a.pol, srun, total, q, acc, cnt, list,
-                                           a.nbr_cap);
+            pair_sums_s<real, BLOCK, NBR>(pair_constants(rp), P, a.pos, a.pol, srun, total, q, acc, cnt, list,
+                                          a.nbr_cap);
         }
         // the rest of the particle's own state, read again (an L1/L2 hit) rather than kept live
         // (spilled at 40 registers) across the pair loop: 64/104 bytes of spill stores/loads per
@@ -755,6 +697,16 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
         r4 ol;
         ol.x = qx, ol.y = qy, ol.z = qz, ol.w = face_to_real(f2, (real)0);
         a.pol_o[q] = ol;
+        // next step's cell key: the surface cell of the new position (one row-record load; looking the
+        // new cell up in the old cell's neighbour descriptor first took the step kernel 4 us longer
+        // at 1M particles), count and scan-tile count (counting sort)
+        bool lost = false;
+        const int key = bucket_of(rp, a.rows, a.ivals, rx, ry, rz, lost);
+        if (lost) st |= ST_CELL;
+        atomicAdd(&a.count[key], 1);
+        a.key_o[q] = key;
+        add_tile(a.tile_sum + (size_t)((*a.d_step + 1) & 1) * a.n_tiles, key);
+
         // order-parameter partials: normalize((r' - c) x v), v / |v|
         const real ax = rx - a.cx, ay = ry - a.cy, az = rz - a.cz;
         const real Lx = ay * vz - az * vy, Ly = az * vx - ax * vz, Lz = ax * vy - ay * vx;
@@ -800,31 +752,6 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
             atomicAdd(&a.phi_acc[((size_t)rep * kPhiCopies + copy) * 6 + k],
                       (unsigned long long)__double2ll_rn((double)ph[k] * ps));
     }
-}
-
-// Next step's cell key of every particle: the surface cell of its new position (row table, then the
-// row's x-intervals), counted into the cell counts and its scan tile's count for the counting sort.
-// A position in no surface cell is the reference's lost particle (status bit 16, the particle goes
-// to the replica's overflow bucket). A kernel of its own rather than the tail of k_step: the two
-// dependent table loads per particle are hidden by many resident warps here (few registers),
-// where at the end of the step kernel they were the last links of a long dependent chain.
-template <typename real>
-__global__ void __launch_bounds__(256) k_key(const R4<real>* __restrict__ pos, const int* __restrict__ ids,
-                                             const RepParams<real>* __restrict__ reps, int local_bits, int single,
-                                             const int2* __restrict__ rows, const int4* __restrict__ ivals,
-                                             int* __restrict__ count, int* __restrict__ key_o,
-                                             int* __restrict__ tile_sum, int n_tiles, const long long* d_step,
-                                             int* status, int N) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= N) return;
-    const R4<real> P = pos[q];
-    const int rep = single ? 0 : (int)((unsigned)ids[q] >> local_bits);
-    bool lost = false;
-    const int key = bucket_of(reps[rep], rows, ivals, P.x, P.y, P.z, lost);
-    if (lost) atomicOr(status, ST_CELL);
-    atomicAdd(&count[key], 1);
-    key_o[q] = key;
-    add_tile(tile_sum + (size_t)((*d_step + 1) & 1) * n_tiles, key);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1157,7 +1084,7 @@ template <typename real, typename I>
 __global__ void k_load_state(const I* i_uv, const I* i_th, const int* i_face, const I* i_r3d,
                              int has_face, int has_r3d, const real* rec, const int4* adj, int G, const int* bs,
                              const int* bf, const int* packed_ids, const RepParams<real>* reps, int local_bits,
-                             const int2* rows, const int4* ivals, R4<real>* pos, R4<real>* pol, R2<real>* uv,
+                             const int4* rows, const int4* ivals, R4<real>* pos, R4<real>* pol, R2<real>* uv,
                              int* ids, R2<real>* vel, int* cnt, int* key, int* count, int N, int* status,
                              const int* flag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1255,11 +1182,20 @@ __global__ void k_place(const double* __restrict__ frec, const double* __restric
     o_th[i] = atan2(wv, wu);
 }
 
-// The run's loop on the device: the handle's loop graph is one conditional WHILE node whose body
-// is one step followed by k_loop_ctl; k_loop_set stores the number of steps before the graph is
-// launched. The body runs while the condition is non-zero: k_loop_ctl counts the steps down and
-// clears the condition after the last one (the host only launches the graph for n >= 1).
-__global__ void k_loop_set(int* left, int n) { *left = n; }
+// The run's loop on the device. The handle's loop graph holds k_loop_arm and two conditional WHILE
+// nodes: the first one's body is a block of steps followed by k_loop_ctl, the second one's body one
+// step followed by k_loop_ctl. Before the graph is launched, k_loop_set stores the number of blocks
+// and of single steps; k_loop_arm sets each loop's condition from its count (a loop whose count is
+// zero does not run), and each k_loop_ctl counts its loop down and clears the condition after the
+// last pass, so every loop ends after the stored number of passes.
+__global__ void k_loop_set(int* left, int blocks, int singles) {
+    left[0] = blocks;
+    left[1] = singles;
+}
+__global__ void k_loop_arm(const int* left, cudaGraphConditionalHandle hb, cudaGraphConditionalHandle h1) {
+    cudaGraphSetConditional(hb, left[0] > 0 ? 1u : 0u);
+    cudaGraphSetConditional(h1, left[1] > 0 ? 1u : 0u);
+}
 __global__ void k_loop_ctl(int* left, cudaGraphConditionalHandle h) {
     const int r = *left - 1;
     *left = r;

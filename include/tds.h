@@ -93,8 +93,9 @@ int tds_ensemble_create(const tds_mesh* mesh, int n_replicas, const int* n_parti
  *   count is <= max(64, cells_per_particle * N_r) (small replicas on a large surface take
  *   coarser cells); default 4.
  * step_block: threads per block of the step kernel, 128 or 256 (default 128).
- * graph_steps: 0 (default): a run of n >= 2 steps is one launch of the handle's loop graph (a
- *   conditional WHILE node around one step; the step count is set on the device before the launch);
+ * graph_steps: 0 (default): a run of n >= 2 steps is one launch of the handle's loop graph
+ *   (conditional WHILE nodes around blocks of 16 steps and single steps; the counts are set on the
+ *   device before the launch);
  *   2..256 (even): runs are launched as captured graphs of this many steps, the rest directly. */
 typedef struct tds_tuning {
     double cells_per_particle;
@@ -239,8 +240,8 @@ int tds_adjoint_run(tds_sim* sim, const tds_adjoint_spec* spec, tds_adjoint_resu
 int tds_adjoint_release(tds_sim* sim);
 /* Per-kernel CUDA-event timing of directly launched steps (graphs are not used while enabled).
  * tds_kernel_times returns, per kernel (0 scan + order-parameter finalize, 1 scatter, 2 order, 3 step,
- * 4 standalone finalize before a series read, 5 next-step cell keys), the summed device time in ms
- * and the launch count since timing was enabled (arrays of 6). */
+ * 4 standalone finalize before a series read), the summed device time in ms and the launch count
+ * since timing was enabled (arrays of 5). */
 int tds_kernel_timing(tds_sim* sim, int enable);
 int tds_kernel_times(tds_sim* sim, double* total_ms, long long* launches);
 /* The CUDA stream every kernel of this handle runs on (cudaStream_t). */
