@@ -63,7 +63,7 @@ GRAD_PARAMS = ("k_rep", "k_adh", "v0", "mu", "tau", "align", "eta")
 
 class _Tuning(C.Structure):
     _fields_ = [("cells_per_particle", C.c_double), ("step_block", C.c_int), ("graph_steps", C.c_int),
-                ("reserved", C.c_int)]
+                ("lanes_per_particle", C.c_int)]
 
 
 class _RefParams(C.Structure):
@@ -250,7 +250,8 @@ class Simulation:
             ps = list(params) if isinstance(params, (list, tuple)) else [params] * len(n)
             self.params = ps
             arr = (_Params * len(n))(*[q.to_c() for q in ps])
-            t = _Tuning(float(tuning["cells_per_particle"]), int(tuning["step_block"]), int(tuning["graph_steps"]), 0)
+            t = _Tuning(float(tuning["cells_per_particle"]), int(tuning["step_block"]), int(tuning["graph_steps"]),
+                        int(tuning.get("lanes_per_particle", 1)))
             rc = L.tds_create_ex(mesh.h, len(n), n.ctypes.data, C.cast(arr, C.c_void_p), C.c_uint64(seed),
                                  int(precision), C.byref(t), C.byref(h))
         elif np.ndim(n_particles) == 0:
@@ -362,7 +363,8 @@ class Simulation:
     def tuning(self):
         t = _Tuning()
         self._check(lib().tds_get_tuning(self.h, C.byref(t)))
-        return dict(cells_per_particle=t.cells_per_particle, step_block=t.step_block, graph_steps=t.graph_steps)
+        return dict(cells_per_particle=t.cells_per_particle, step_block=t.step_block, graph_steps=t.graph_steps,
+                    lanes_per_particle=t.lanes_per_particle)
 
     def set_params(self, params):
         """New model parameters (one Params, or one per replica); radius and r_max must not change."""
@@ -598,7 +600,8 @@ def autotune(mesh, params, n_particles, seed=0, precision=32, trial_steps=64):
                             int(trial_steps), C.byref(t), C.byref(rate))
     if rc != TDS_OK:
         raise TdsError(rc, "autotune failed")
-    return dict(cells_per_particle=t.cells_per_particle, step_block=t.step_block, graph_steps=t.graph_steps), rate.value
+    return (dict(cells_per_particle=t.cells_per_particle, step_block=t.step_block, graph_steps=t.graph_steps,
+                 lanes_per_particle=t.lanes_per_particle), rate.value)
 
 
 def debug_seam_wrap(uv_old, uv, theta=None, vel=None, precision=64):

@@ -130,6 +130,7 @@ struct tds_sim {
     int* loop_left = nullptr;  // device: [0] step blocks, [1] single steps left in the running loop graph
     int graph_steps = 0;         // 0: loop graph; 2..256 (even): steps per captured chunk (tuning)
     int step_block = 128;        // threads per k_step block (tuning: 128 or 256)
+    int lanes = 1;               // lanes per particle in k_step (tuning: 1, 2 or 4; > 1 with 128-thread blocks)
     double cells_per_particle = 4.0;  // cell-level rule (tuning): finest level with C <= max(64, this * N_r)
     double origin[3] = {0, 0, 0};
     std::vector<void*> allocs;
@@ -562,8 +563,13 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
     }
     {
         KernelTimer kt(s, 3);
+        const long long lanes = (long long)s->N * s->lanes;
         if (nbr_list)
             tdsk::k_step<real, 128, true><<<(s->N + 127) / 128, 128, 0, st>>>(a);
+        else if (s->lanes == 2)
+            tdsk::k_step<real, 128, false, 2><<<(unsigned)((lanes + 127) / 128), 128, 0, st>>>(a);
+        else if (s->lanes == 4)
+            tdsk::k_step<real, 128, false, 4><<<(unsigned)((lanes + 127) / 128), 128, 0, st>>>(a);
         else if (s->step_block == 128)
             tdsk::k_step<real, 128><<<(s->N + 127) / 128, 128, 0, st>>>(a);
         else
@@ -1376,12 +1382,15 @@ int create_impl(const tds_mesh* mesh, int R, const int* n, const tds_params* prm
     s->mesh = mesh;
     s->precision = precision;
     if (tune) {
+        const int lanes = tune->lanes_per_particle ? tune->lanes_per_particle : 1;
         if (!(tune->cells_per_particle > 0) || (tune->step_block != 128 && tune->step_block != 256) ||
-            (tune->graph_steps != 0 && (tune->graph_steps < 2 || tune->graph_steps % 2 || tune->graph_steps > 256)))
+            (tune->graph_steps != 0 && (tune->graph_steps < 2 || tune->graph_steps % 2 || tune->graph_steps > 256)) ||
+            (lanes != 1 && lanes != 2 && lanes != 4) || (lanes > 1 && tune->step_block != 128))
             return TDS_ERR_ARG;
         s->cells_per_particle = tune->cells_per_particle;
         s->step_block = tune->step_block;
         s->graph_steps = tune->graph_steps;
+        s->lanes = lanes;
     }
     s->rsz = precision == 32 ? 4 : 8;
     s->R = R;
@@ -1527,47 +1536,63 @@ int tds_get_tuning(const tds_sim* s, tds_tuning* out) {
     out->cells_per_particle = s->cells_per_particle;
     out->step_block = s->step_block;
     out->graph_steps = s->graph_steps;
+    out->lanes_per_particle = s->lanes;
     return TDS_OK;
 }
 
 int tds_autotune(const tds_mesh* mesh, int n_replicas, const int* n_particles, const tds_params* params,
                  uint64_t seed, int precision, int trial_steps, tds_tuning* best, double* best_rate) {
     if (!mesh || !n_particles || !params || !best || trial_steps < 1) return TDS_ERR_ARG;
-    // candidates: the cell-level rule, the step block and the graph chunk; each is timed on the
-    // caller's workload (created, placed, warmed up, then trial_steps graph-launched steps)
-    const double cpp[] = {1.0, 4.0, 16.0};
-    const int blocks[] = {128, 256};
-    const int chunks[] = {0, 16};  // the loop graph, or graphs of 16 steps
+    // candidates are timed on the caller's workload (created, placed, warmed up, then trial_steps
+    // graph-launched steps, the best of two timings): first the cell-level rule x the step block
+    // (one lane per particle, the loop graph), then, on the best of those, 2 and 4 lanes per
+    // particle and graphs of 16 steps
     double best_r = -1;
-    tds_tuning bt{4.0, 128, 0, 0};
+    tds_tuning bt{4.0, 128, 0, 1};
     long long total = 0;
     for (int r = 0; r < n_replicas; ++r) total += n_particles[r];
-    for (double c : cpp)
-        for (int b : blocks)
-            for (int g : chunks) {
-                tds_tuning t{c, b, g, 0};
-                tds_sim* s = nullptr;
-                int rc = create_impl(mesh, n_replicas, n_particles, params, seed, precision, &s, &t);
-                if (rc) return rc;
-                cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto time_one = [&](const tds_tuning& t, double* rate) -> int {
+        tds_sim* s = nullptr;
+        int rc = create_impl(mesh, n_replicas, n_particles, params, seed, precision, &s, &t);
+        if (rc) return rc;
+        const int g = t.graph_steps;
+        const int steps = g ? (trial_steps + g - 1) / g * g : trial_steps;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        rc = tds_start(s);
+        if (!rc) rc = tds_step(s, g ? g : 16, nullptr);  // warm-up: graph capture
+        double best_ms = 0;
+        if (!rc && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
+            for (int rep = 0; rep < 2 && !rc; ++rep) {
                 float ms = 0;
-                const int steps = g ? (trial_steps + g - 1) / g * g : trial_steps;
-                rc = tds_start(s);
-                if (!rc) rc = tds_step(s, g ? g : 16, nullptr);  // warm-up: graph capture
-                if (!rc && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
-                    cudaEventRecord(e0, s->stream);
-                    rc = tds_step_async(s, steps);
-                    cudaEventRecord(e1, s->stream);
-                    if (!rc) rc = tds_sync(s);
-                    if (!rc) cudaEventElapsedTime(&ms, e0, e1);
-                }
-                if (e0) cudaEventDestroy(e0);
-                if (e1) cudaEventDestroy(e1);
-                tds_destroy(s);
-                if (rc) return rc;
-                const double rate = ms > 0 ? (double)total * steps / (ms * 1e-3) : 0.0;
-                if (rate > best_r) best_r = rate, bt = t;
+                cudaEventRecord(e0, s->stream);
+                rc = tds_step_async(s, steps);
+                cudaEventRecord(e1, s->stream);
+                if (!rc) rc = tds_sync(s);
+                if (!rc) cudaEventElapsedTime(&ms, e0, e1);
+                if (ms > 0 && (best_ms == 0 || ms < best_ms)) best_ms = ms;
             }
+        }
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        tds_destroy(s);
+        *rate = best_ms > 0 ? (double)total * steps / (best_ms * 1e-3) : 0.0;
+        return rc;
+    };
+    for (double c : {1.0, 4.0, 16.0})
+        for (int b : {128, 256}) {
+            const tds_tuning t{c, b, 0, 1};
+            double rate = 0;
+            if (int rc = time_one(t, &rate)) return rc;
+            if (rate > best_r) best_r = rate, bt = t;
+        }
+    const tds_tuning base = bt;
+    const tds_tuning more[] = {{base.cells_per_particle, 128, 0, 2}, {base.cells_per_particle, 128, 0, 4},
+                               {base.cells_per_particle, base.step_block, 16, 1}};
+    for (const tds_tuning& t : more) {
+        double rate = 0;
+        if (int rc = time_one(t, &rate)) return rc;
+        if (rate > best_r) best_r = rate, bt = t;
+    }
     *best = bt;
     if (best_rate) *best_rate = best_r;
     return TDS_OK;

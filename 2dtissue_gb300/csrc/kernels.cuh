@@ -541,16 +541,57 @@ __device__ __forceinline__ void pair_sums_s(const PairC<real>& pc, const R4<real
     }
 }
 
+// Several lanes per particle (LPP = 2 or 4, a tuning choice): lane `sub` of the particle's group
+// takes the candidates sub, sub + LPP, sub + 2 LPP, ... of the visiting order, one per iteration,
+// and sums their terms in that order; the group's partial sums are then added over the lanes with a
+// fixed butterfly, so every lane of the group holds the same totals and every run gives the same
+// bits (a different rounding order from the one-lane loop, the same sums to rounding).
+template <typename real, int BLOCK, int LPP>
+__device__ __forceinline__ void pair_sums_lanes(const PairC<real>& pc, const R4<real>& P,
+                                                const R4<real>* __restrict__ pos, const R4<real>* __restrict__ pol,
+                                                const int2* srun, int total, int self, int sub, real (&acc)[6],
+                                                int& cnt) {
+    const int mine = total > sub ? (total - sub + LPP - 1) / LPP : 0;
+    const int2* sp = srun;
+    int t = 0, left = 0;
+    if (total > 0) {
+        const int2 x0 = *sp;
+        t = x0.x, left = x0.y;
+    }
+    int skip = sub;
+    for (int i = 0; i < mine; ++i) {
+        while (skip >= left) {  // the table holds non-empty runs only; `mine` keeps this in range
+            skip -= left;
+            sp += BLOCK;
+            const int2 x = *sp;
+            t = x.x, left = x.y;
+        }
+        t += skip, left -= skip;
+        const int j = t++;
+        --left;
+        skip = LPP - 1;
+        const R4<real> Q = pos[j];
+        if (pair_d2(P, Q) < pc.r_max2 && j != self) pair_add(pc, P, Q, pol[j], acc, cnt);
+    }
+}
+
 // BLOCK: threads per block (a tuning choice: 128 or 256); the register budget is the same either
 // way (6 blocks of 256, 12 of 128 per SM in FP32: 40 registers; 6 rather than 5 blocks of 256 took the
 // step from 170.9 to 168.6 us at 1M particles).
 // NBR: the test hook's instantiation that also exports each particle's neighbours (sorted slots,
 // converted to particle indices by k_nbr_ids); the production launches use NBR = false.
-template <typename real, int BLOCK, bool NBR = false>
+// LPP: lanes per particle (1, 2 or 4; 32 / LPP particles per warp). With LPP > 1 the lanes of a
+// particle split its candidates (pair_sums_lanes), then all of them run the particle's update on
+// the same sums and the group's first lane ("lead") stores the results and does the atomics.
+template <typename real, int BLOCK, bool NBR = false, int LPP = 1>
 __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLOCK) k_step(const StepArgs<real> a) {
     typedef R4<real> r4;
-    const int q = blockIdx.x * BLOCK + threadIdx.x;
+    static_assert(LPP == 1 || LPP == 2 || LPP == 4, "1, 2 or 4 lanes per particle");
+    static_assert(!(NBR && LPP > 1), "the neighbour export runs one lane per particle");
+    const int q = (int)((blockIdx.x * BLOCK + threadIdx.x) / LPP);
+    const int sub = LPP > 1 ? (int)(threadIdx.x % LPP) : 0;
     const bool active = q < a.N;
+    const bool lead = active && sub == 0;
     int rep = -1;
     real ph[6] = {0, 0, 0, 0, 0, 0};
     int st = 0;
@@ -596,11 +637,23 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
         // memory
         int* list = NBR ? a.nbr_list + (size_t)(rp.off + (int)((unsigned)id & ((1u << a.local_bits) - 1u))) * a.nbr_cap
                         : nullptr;
-        if (a.single)
-            pair_sums_s<real, BLOCK, NBR>(a.pc0, P, a.pos, a.pol, srun, total, q, acc, cnt, list, a.nbr_cap);
-        else
-            pair_sums_s<real, BLOCK, NBR>(pair_constants(rp), P, a.pos, a.pol, srun, total, q, acc, cnt, list,
-                                          a.nbr_cap);
+        if (LPP == 1) {
+            if (a.single)
+                pair_sums_s<real, BLOCK, NBR>(a.pc0, P, a.pos, a.pol, srun, total, q, acc, cnt, list, a.nbr_cap);
+            else
+                pair_sums_s<real, BLOCK, NBR>(pair_constants(rp), P, a.pos, a.pol, srun, total, q, acc, cnt, list,
+                                              a.nbr_cap);
+        } else {
+            pair_sums_lanes<real, BLOCK, LPP>(a.single ? a.pc0 : pair_constants(rp), P, a.pos, a.pol, srun, total, q,
+                                              sub, acc, cnt);
+            const unsigned gm = ((1u << LPP) - 1u) << ((threadIdx.x & 31) & ~(unsigned)(LPP - 1));
+#pragma unroll
+            for (int o = 1; o < LPP; o <<= 1) {
+#pragma unroll
+                for (int k = 0; k < 6; ++k) acc[k] += __shfl_xor_sync(gm, acc[k], o);
+                cnt += __shfl_xor_sync(gm, cnt, o);
+            }
+        }
         }
         // the rest of the particle's own state, read again (an L1/L2 hit) rather than kept live
         // (spilled at 40 registers) across the pair loop: 64/104 bytes of spill stores/loads per
@@ -608,8 +661,10 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
         const r4 PL = reload(a.pol, q);
         const R2<real> U = reload(a.uv, q);
         const int id = reload(a.ids, q);
-        a.ids_o[q] = id;
-        a.cnt_o[q] = cnt;
+        if (lead) {
+            a.ids_o[q] = id;
+            a.cnt_o[q] = cnt;
+        }
         const int f = real_to_face(PL.w);
         rep = (int)((unsigned)id >> a.local_bits);
         const unsigned local = (unsigned)id & ((1u << a.local_bits) - 1u);
@@ -668,10 +723,10 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
             // outputs are stored as soon as they are known, so that nothing is live for them
             R2<real> vo;
             vo.x = vu, vo.y = vv;
-            a.vel_o[q] = vo;
+            if (lead) a.vel_o[q] = vo;
             R2<real> uo;
             uo.x = u2, uo.y = v2;
-            a.uv_o[q] = uo;
+            if (lead) a.uv_o[q] = uo;
         }
         int mode = 0;
         const int f2 = locate(a.rec, a.adj, a.G, a.bin_start, a.bin_faces, u2, v2, f, mode);
@@ -693,43 +748,45 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
 
         r4 o;
         o.x = rx, o.y = ry, o.z = rz, o.w = th;
-        a.pos_o[q] = o;
+        if (lead) a.pos_o[q] = o;
         r4 ol;
         ol.x = qx, ol.y = qy, ol.z = qz, ol.w = face_to_real(f2, (real)0);
-        a.pol_o[q] = ol;
+        if (lead) a.pol_o[q] = ol;
         // next step's cell key: the surface cell of the new position (one row-record load; looking the
         // new cell up in the old cell's neighbour descriptor first took the step kernel 4 us longer
         // at 1M particles), count and scan-tile count (counting sort)
         bool lost = false;
         const int key = bucket_of(rp, a.rows, a.ivals, rx, ry, rz, lost);
         if (lost) st |= ST_CELL;
-        atomicAdd(&a.count[key], 1);
-        a.key_o[q] = key;
-        add_tile(a.tile_sum + (size_t)((*a.d_step + 1) & 1) * a.n_tiles, key);
+        if (lead) {
+            atomicAdd(&a.count[key], 1);
+            a.key_o[q] = key;
+            add_tile(a.tile_sum + (size_t)((*a.d_step + 1) & 1) * a.n_tiles, key);
+        }
 
         // order-parameter partials: normalize((r' - c) x v), v / |v|
         const real ax = rx - a.cx, ay = ry - a.cy, az = rz - a.cz;
         const real Lx = ay * vz - az * vy, Ly = az * vx - ax * vz, Lz = ax * vy - ay * vx;
         const real Ln2 = Lx * Lx + Ly * Ly + Lz * Lz;
-        if (Ln2 > (real)0) {
+        if (lead && Ln2 > (real)0) {
             const real iL = d_rsqrt(Ln2);
             ph[0] = Lx * iL, ph[1] = Ly * iL, ph[2] = Lz * iL;
         }
-        if (vn2 > (real)0) {
+        if (lead && vn2 > (real)0) {
             ph[3] = vx * ivn, ph[4] = vy * ivn, ph[5] = vz * ivn;
         }
     }
-    if (st) atomicOr(a.status, st);
-    if (q == 0) *a.phi_pending = 1;
+    if (st && lead) atomicOr(a.status, st);
+    if (q == 0 && sub == 0) *a.phi_pending = 1;
 
     // order-parameter reduction: warp sum (same replica) -> atomics on one of kPhiCopies slots
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const unsigned amask = __ballot_sync(FULL, active);
+    const unsigned amask = __ballot_sync(FULL, lead);
     if (!amask) return;
     const int rep0 = __shfl_sync(FULL, rep, __ffs(amask) - 1);
-    const bool same = __all_sync(FULL, !active || rep == rep0);
-    const int copy = (q >> 5) % kPhiCopies;
+    const bool same = __all_sync(FULL, !lead || rep == rep0);
+    const int copy = (int)(((blockIdx.x * BLOCK + threadIdx.x) >> 5) % kPhiCopies);
     if (same) {
         // fixed butterfly over fixed lanes: the warp sum is the same on every run
 #pragma unroll
@@ -745,7 +802,7 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
             const long long iv = __double2ll_rn((double)v * a.reps[rep0].phiscale);
             atomicAdd(&a.phi_acc[((size_t)rep0 * kPhiCopies + copy) * 6 + lane], (unsigned long long)iv);
         }
-    } else if (active) {
+    } else if (lead) {
         const double ps = a.reps[rep].phiscale;
 #pragma unroll
         for (int k = 0; k < 6; ++k)

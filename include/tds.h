@@ -96,20 +96,25 @@ int tds_ensemble_create(const tds_mesh* mesh, int n_replicas, const int* n_parti
  * graph_steps: 0 (default): a run of n >= 2 steps is one launch of the handle's loop graph
  *   (conditional WHILE nodes around blocks of 16 steps and single steps; the counts are set on the
  *   device before the launch);
- *   2..256 (even): runs are launched as captured graphs of this many steps, the rest directly. */
+ *   2..256 (even): runs are launched as captured graphs of this many steps, the rest directly.
+ * lanes_per_particle: lanes of the step kernel per particle, 1 (default; 32 particles per warp),
+ *   2 or 4 (16 or 8 particles per warp: the lanes split the particle's candidates and add their
+ *   partial sums in a fixed order; needs step_block 128); 0 means 1. */
 typedef struct tds_tuning {
     double cells_per_particle;
     int step_block;
     int graph_steps;
-    int reserved;
+    int lanes_per_particle;
 } tds_tuning;
 /* tds_ensemble_create with a tuning (NULL = defaults); n_replicas = 1 for a plain system. */
 int tds_create_ex(const tds_mesh* mesh, int n_replicas, const int* n_particles, const tds_params* params,
                   uint64_t seed, int precision, const tds_tuning* tuning, tds_sim** out);
 int tds_get_tuning(const tds_sim* sim, tds_tuning* out);
-/* Autotuner: creates the workload with each candidate tuning (cells_per_particle 1, 4, 16 x
- * step_block 128, 256 x graph_steps 0, 16), places it, and times trial_steps graph-launched steps
- * on the device; returns the fastest tuning and its particle-steps/s. */
+/* Autotuner: creates the workload with each candidate tuning, places it, and times trial_steps
+ * graph-launched steps on the device (best of two timings): cells_per_particle 1, 4, 16 x
+ * step_block 128, 256 (one lane per particle, the loop graph), then on the fastest of those
+ * lanes_per_particle 2 and 4 and graph_steps 16; returns the fastest tuning and its
+ * particle-steps/s. */
 int tds_autotune(const tds_mesh* mesh, int n_replicas, const int* n_particles, const tds_params* params,
                  uint64_t seed, int precision, int trial_steps, tds_tuning* best, double* best_rate);
 

@@ -1,6 +1,6 @@
 """Tuning choices (tds_create_ex) and the autotuner (tds_autotune): the step block changes no
-bit; a coarser cell level keeps per-step parity with the oracle; the autotuner returns one of its
-candidates with a positive rate."""
+bit; a coarser cell level and 2 or 4 lanes per particle keep per-step parity with the oracle; the
+autotuner returns one of its candidates with a positive rate."""
 import numpy as np
 import pytest
 
@@ -50,8 +50,44 @@ def test_autotune_returns_a_candidate(tg, mesh_l4):
     ns = [200, 800, 3000]
     t, rate = tg.autotune(mesh_l4, [tg.Params()] * 3, ns, trial_steps=32)
     assert t["cells_per_particle"] in (1.0, 4.0, 16.0) and t["step_block"] in (128, 256)
-    assert t["graph_steps"] in (0, 16) and rate > 0
+    assert t["graph_steps"] in (0, 16) and t["lanes_per_particle"] in (1, 2, 4) and rate > 0
     sim = tg.Simulation(mesh_l4, [tg.Params()] * 3, ns, tuning=t)
     sim.start()
     sim.step(16)
     assert sim.status() == 0
+
+
+@pytest.mark.parametrize("lanes", [2, 4])
+@pytest.mark.parametrize("precision", [32, 64])
+def test_lanes_per_particle_keep_parity(tg, orc, mesh_l4, lanes, precision):
+    """2 and 4 lanes per particle (16 or 8 particles per warp): per-step parity with the oracle on a
+    dense system, and two runs give the same bits (the lanes' partial sums are added in a fixed
+    order)."""
+    om, arr = oracle_mesh(orc, mesh_l4)
+    cen = arr["v3"].mean(0)
+    p = tg.Params()
+    tun = dict(cells_per_particle=4.0, step_block=128, graph_steps=0, lanes_per_particle=lanes)
+    runs = []
+    for _ in range(2):
+        sim = tg.Simulation(mesh_l4, p, 2000, seed=5, precision=precision, tuning=tun)
+        assert sim.tuning()["lanes_per_particle"] == lanes
+        sim.start()
+        sim.step(3)
+        g0 = sim.get_state()
+        sim.step(1)
+        g1 = sim.get_state()
+        out = compare_step(orc, om, p.oracle_dict(), g0, g1, 3, 5, precision, centroid=cen)
+        assert out["nbr"].mean() > 1.0
+        sim.step(20)
+        runs.append(sim.get_state())
+    for k in runs[0]:
+        np.testing.assert_array_equal(runs[0][k], runs[1][k])
+
+
+def test_lanes_need_128_thread_blocks(tg, mesh_l4):
+    with pytest.raises(tg.TdsError):
+        tg.Simulation(mesh_l4, tg.Params(), 100, tuning=dict(cells_per_particle=4.0, step_block=256, graph_steps=0,
+                                                            lanes_per_particle=2))
+    with pytest.raises(tg.TdsError):
+        tg.Simulation(mesh_l4, tg.Params(), 100, tuning=dict(cells_per_particle=4.0, step_block=128, graph_steps=0,
+                                                            lanes_per_particle=3))
