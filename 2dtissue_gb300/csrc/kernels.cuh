@@ -1133,19 +1133,23 @@ __global__ void k_clear_counts(int* __restrict__ count, long long M, int* __rest
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_tile_sum; i += stride) tile_sum[i] = 0;
 }
 
-// Loads a state given in id order (I: double, or float for an FP32 state) into slots = global
-// index; locates faces that are < 0, maps r3d when it is not given, derives the 3D polarity, and
-// counts the particle into its cell bucket for the next step's counting sort (counts must be zero
-// on entry).
+// Loads a state given in id order (I: double, or float for an FP32 state): particle i goes to
+// slot_of[i], the slot it holds in the handle's current order (any permutation gives the same next
+// step, whose counting sort orders the particles by cell and id; the current order keeps the
+// writes, the face records and the cell rows the load touches, and the next step's sort, spatially
+// coherent); locates faces that are < 0, maps r3d when it is not given, derives the 3D polarity,
+// and counts the particle into its cell bucket for the next step's counting sort (counts must be
+// zero on entry).
 template <typename real, typename I>
 __global__ void k_load_state(const I* i_uv, const I* i_th, const int* i_face, const I* i_r3d,
                              int has_face, int has_r3d, const real* rec, const int4* adj, int G, const int* bs,
                              const int* bf, const int* packed_ids, const RepParams<real>* reps, int local_bits,
-                             const int4* rows, const int4* ivals, R4<real>* pos, R4<real>* pol, R2<real>* uv,
-                             int* ids, R2<real>* vel, int* cnt, int* key, int* count, int N, int* status,
-                             const int* flag) {
+                             const int4* rows, const int4* ivals, const int* __restrict__ slot_of, R4<real>* pos,
+                             R4<real>* pol, R2<real>* uv, int* ids, R2<real>* vel, int* cnt, int* key, int* count,
+                             int N, int* status, const int* flag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N || flag[0]) return;
+    const int sl = slot_of[i];
     const real u = (real)i_uv[2 * i], v = (real)i_uv[2 * i + 1];
     int f = has_face ? i_face[i] : -1;
     if (f < 0) {
@@ -1161,24 +1165,24 @@ __global__ void k_load_state(const I* i_uv, const I* i_th, const int* i_face, co
         face_map(h, u, v, P.x, P.y, P.z);
     }
     P.w = (real)i_th[i];
-    pos[i] = P;
+    pos[sl] = P;
     R4<real> L;
     polarity3(h, P.w, L.x, L.y, L.z);
     L.w = face_to_real(f, (real)0);
-    pol[i] = L;
+    pol[sl] = L;
     R2<real> U;
     U.x = u, U.y = v;
-    uv[i] = U;
+    uv[sl] = U;
     const int id = packed_ids[i];
-    ids[i] = id;
+    ids[sl] = id;
     R2<real> Z;
     Z.x = 0, Z.y = 0;
-    vel[i] = Z;
-    cnt[i] = 0;
+    vel[sl] = Z;
+    cnt[sl] = 0;
     bool lost = false;
     const int k = bucket_of(reps[(unsigned)id >> local_bits], rows, ivals, P.x, P.y, P.z, lost);
     if (lost) atomicOr(status, ST_CELL);
-    key[i] = k;
+    key[sl] = k;
     atomicAdd(&count[k], 1);
 }
 
