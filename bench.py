@@ -384,7 +384,8 @@ def ensemble_leg(tg, steps=50, sample=64, autotune=False, replicas=4096):
     sim_tuning = sim.tuning()
     sim.close()
     # one by one: a seeded sample of replicas, each its own plain handle, each replica's steps
-    # launched as the library launches a plain system's steps, one replica after the other
+    # launched as the library launches a plain system's steps (one loop-graph launch), one replica
+    # after the other (each run waited for before the next replica starts)
     pick = np.sort(np.random.default_rng(1).choice(len(ns), min(sample, len(ns)), replace=False))
     sims = [tg.Simulation(mesh, ps[i], ns[i], seed=int(i), precision=32) for i in pick]
     for s_ in sims:
@@ -394,9 +395,14 @@ def ensemble_leg(tg, steps=50, sample=64, autotune=False, replicas=4096):
     steps1 = max(16, steps // 16 * 16)
     t0 = time.perf_counter()
     for s_ in sims:
+        s_.step(steps1)
+    one_by_one = int(n[pick].sum()) * steps1 / (time.perf_counter() - t0)
+    # the same handles' runs enqueued on their own streams without waiting (they may overlap)
+    t0 = time.perf_counter()
+    for s_ in sims:
         s_.step_async(steps1)
     torch.cuda.synchronize()
-    one_by_one = int(n[pick].sum()) * steps1 / (time.perf_counter() - t0)
+    concurrent = int(n[pick].sum()) * steps1 / (time.perf_counter() - t0)
     # the same handles interleaved step by step (one direct launch sequence per replica per step)
     t0 = time.perf_counter()
     for _ in range(8):
@@ -414,7 +420,10 @@ def ensemble_leg(tg, steps=50, sample=64, autotune=False, replicas=4096):
                        "faces": mesh.F},
             "one_by_one": {"value": one_by_one, "replicas_sampled": len(pick), "steps": steps1,
                            "path": "each sampled replica in its own plain handle, its steps launched as a plain "
-                                   "system's (CUDA graphs), one replica after the other"},
+                                   "system's (one loop-graph launch), one replica after the other, each run "
+                                   "waited for"},
+            "concurrent_streams": {"value": concurrent,
+                                   "path": "the same handles' runs enqueued on their own streams without waiting"},
             "interleaved_one_by_one": {"value": interleaved, "steps": 8,
                                        "path": "the same handles, one step of each replica in turn"},
             "batched_over_one_by_one": batched / one_by_one,
@@ -601,7 +610,7 @@ def run_gpu(args):
     # face's chart map of the chart position; tds_set_state derives it on the device when r3d is
     # NULL, bit for bit as the step computes it)
     hin = sim.get_state()
-    e2e_steps = max(3, min(args.steps, 100))
+    e2e_steps = 100  # the loop's own sample: long enough that host-side jitter averages out
 
     def end_to_end(fdt):
         """Per step: state upload, one step, state download, through the state views of float
@@ -756,7 +765,7 @@ def run_profile_adjoint(args):
     ns = [int(x) for x in rng.integers(1000, 20001, size=R)]
     ps = [tg.Params(v0=float(rng.uniform(0.5, 1.5)), k_rep=float(rng.uniform(5, 20)), tau=float(rng.uniform(0.5, 2)),
                     eta=float(rng.uniform(0.1, 1.0))) for _ in range(R)]
-    sim = tg.Simulation(mesh, ps, ns, seed=1, precision=32)
+    sim = tg.Simulation(mesh, ps, ns, seed=1, precision=32, tuning=PROFILE_TUNING)
     sim.start()
     s0 = sim.get_state()
     T = args.steps
@@ -765,12 +774,18 @@ def run_profile_adjoint(args):
     sim.close()
 
 
+# ncu cannot profile the kernel nodes of a graph that holds conditional nodes (the loop graph), so
+# the profiling drivers launch the steps as graphs of 16 steps (the same kernels)
+PROFILE_TUNING = dict(cells_per_particle=4.0, step_block=128, graph_steps=16, lanes_per_particle=1)
+
+
 def run_profile(args):
-    """Minimal driver for ncu: the 1M-particle system, `warmup` steps, then `steps` steps; no timing."""
+    """Minimal driver for ncu: the 1M-particle system, `warmup` steps, then `steps` steps (graphs of
+    16 steps); no timing."""
     import torch
     tg = importlib.import_module("2dtissue_gb300")
     mesh, p, n, _ = workload_1m(tg)
-    sim = tg.Simulation(mesh, p, n, seed=0, precision=32)
+    sim = tg.Simulation(mesh, p, n, seed=0, precision=32, tuning=PROFILE_TUNING)
     sim.start()
     sim.step(args.warmup)
     sim.step_async(args.steps)
@@ -785,7 +800,7 @@ def run_profile_e2e(args):
     import torch
     tg = importlib.import_module("2dtissue_gb300")
     mesh, p, n, _ = workload_1m(tg)
-    sim = tg.Simulation(mesh, p, n, seed=0, precision=32)
+    sim = tg.Simulation(mesh, p, n, seed=0, precision=32, tuning=PROFILE_TUNING)
     sim.start()
     sim.step(args.warmup)
     hin = sim.get_state(dtype=np.float32)
