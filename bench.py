@@ -794,6 +794,24 @@ def run_profile(args):
     sim.close()
 
 
+def run_profile_ensemble(args):
+    """Minimal driver for ncu: the 4,096-replica ensemble of the ensemble leg, placed, `warmup` steps,
+    then `steps` steps (graphs of 16 steps); no timing."""
+    import torch
+    tg = importlib.import_module("2dtissue_gb300")
+    ens = importlib.import_module("2dtissue_gb300.ensemble")
+    mesh = tg.Mesh.ellipsoid(4, (4.0, 2.0, 2.0))
+    n, eta, v0 = ens.ragged_replicas(seed=0, n_replicas=4096)
+    ps = [tg.Params(radius=0.05, r_max=0.12, v0=float(v), eta=float(e), dt=0.02) for e, v in zip(eta, v0)]
+    sim = tg.Simulation(mesh, ps, [int(x) for x in n], seed=0, precision=32, tuning=PROFILE_TUNING)
+    sim.start()
+    sim.step(args.warmup)
+    sim.step_async(args.steps)
+    torch.cuda.synchronize()
+    assert sim.status() == 0
+    sim.close()
+
+
 def run_profile_e2e(args):
     """Minimal driver for ncu: the 1M-particle system, then `steps` iterations of the end-to-end loop
     (pinned FP32-view upload of uv, theta, face; one step; pinned FP32-view download); no timing."""
@@ -845,6 +863,8 @@ def main():
     if args.profile:
         if args.e2e:
             return run_profile_e2e(args)
+        if args.workload == "ensemble":
+            return run_profile_ensemble(args)
         return run_profile_adjoint(args) if args.workload == "adjoint_batched" else run_profile(args)
     if args.impl != "reference":
         tg = None
