@@ -376,10 +376,9 @@ int alloc_state(tds_sim* s) {
     for (int r = 0; r < s->R; ++r)
         for (int i = 0; i < s->n_rep[r]; ++i) pid[s->off[r] + i] = (int)(((unsigned)r << s->local_bits) | (unsigned)i);
     CK(cudaMemcpy(s->packed_ids, pid.data(), N * sizeof(int), cudaMemcpyHostToDevice));
-    // slot of each particle in the current order (rewritten by every read-back): the identity until
-    // the first one; state loads place particle i in slot perm[i]
-    for (size_t i = 0; i < N; ++i) pid[i] = (int)i;
-    CK(cudaMemcpy(s->perm, pid.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    // the current order's ids by slot start as the identity order (state loads fill each slot with
+    // the particle it holds, so the array is a permutation of the packed ids from here on)
+    CK(cudaMemcpy(s->ids[0], pid.data(), N * sizeof(int), cudaMemcpyHostToDevice));
     return TDS_OK;
 }
 
@@ -762,8 +761,8 @@ int load_from_staging(tds_sim* s, int b, bool has_face, bool has_r3d, bool sync,
     tdsk::k_clear_counts<<<nc, 256, 0, s->stream>>>(s->count, s->M, s->tile_sum, 2 * s->n_tiles, s->load_flag);
     tdsk::k_load_state<real, I><<<nb, 256, 0, s->stream>>>(
         in, in + 2 * N, s->in_i[b], in + 3 * N, has_face, has_r3d, (const real*)s->rec, s->adj, s->G,
-        s->bin_start, s->bin_faces, s->packed_ids, (const RepParams<real>*)s->reps, s->local_bits, s->rows, s->ivals,
-        s->perm, (R4<real>*)s->pos[0], (R4<real>*)s->pol[0], (R2<real>*)s->uv[0], s->ids[0], (R2<real>*)s->vel[0], s->cnt[0],
+        s->bin_start, s->bin_faces, (const RepParams<real>*)s->reps, s->local_bits, s->rows, s->ivals, s->ids[0],
+        (R4<real>*)s->pos[0], (R4<real>*)s->pol[0], (R2<real>*)s->uv[0], s->ids[0], (R2<real>*)s->vel[0], s->cnt[0],
         s->key[0], s->count, s->N, s->status, s->load_flag);
     tdsk::k_tile_sums<<<s->n_tiles, tdsk::kScanThreads, 0, s->stream>>>(s->count, s->M, s->tile_sum, s->n_tiles,
                                                                          s->d_step, s->load_flag);
@@ -838,8 +837,7 @@ int start_device(tds_sim* s) {
 }
 
 // The current state in global index order into o_* (device arrays) on the compute stream; the
-// slot table goes through the handle's perm array (which the next state load also uses: it places
-// each particle in the slot it holds now).
+// slot table goes through the handle's perm array.
 template <typename real, typename O>
 void gather_state(tds_sim* s, O* o_uv, O* o_th, int* o_face, O* o_r3d, O* o_vel, int* o_cnt) {
     const int c = s->cur;

@@ -1133,23 +1133,26 @@ __global__ void k_clear_counts(int* __restrict__ count, long long M, int* __rest
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_tile_sum; i += stride) tile_sum[i] = 0;
 }
 
-// Loads a state given in id order (I: double, or float for an FP32 state): particle i goes to
-// slot_of[i], the slot it holds in the handle's current order (any permutation gives the same next
-// step, whose counting sort orders the particles by cell and id; the current order keeps the
-// writes, the face records and the cell rows the load touches, and the next step's sort, spatially
-// coherent); locates faces that are < 0, maps r3d when it is not given, derives the 3D polarity,
-// and counts the particle into its cell bucket for the next step's counting sort (counts must be
-// zero on entry).
+// Loads a state given in id order (I: double, or float for an FP32 state), one thread per slot:
+// slot s takes the particle it holds in the handle's current order (slot_ids: the current packed
+// ids by slot, a permutation of the handle's particles from creation on). Any arrangement gives the
+// same next step, whose counting sort orders the particles by cell and id; keeping the current one
+// makes the writes coalesced and the face-record and cell-row reads spatially coherent (the input
+// is read by particle index, from the staging the upload just wrote), and the next step's sort
+// starts from a sorted order. Locates faces that are < 0, maps r3d when it is not given, derives
+// the 3D polarity, and counts the particle into its cell bucket for the next step's counting sort
+// (counts must be zero on entry).
 template <typename real, typename I>
 __global__ void k_load_state(const I* i_uv, const I* i_th, const int* i_face, const I* i_r3d,
                              int has_face, int has_r3d, const real* rec, const int4* adj, int G, const int* bs,
-                             const int* bf, const int* packed_ids, const RepParams<real>* reps, int local_bits,
-                             const int4* rows, const int4* ivals, const int* __restrict__ slot_of, R4<real>* pos,
-                             R4<real>* pol, R2<real>* uv, int* ids, R2<real>* vel, int* cnt, int* key, int* count,
-                             int N, int* status, const int* flag) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N || flag[0]) return;
-    const int sl = slot_of[i];
+                             const int* bf, const RepParams<real>* reps, int local_bits, const int4* rows,
+                             const int4* ivals, const int* slot_ids, R4<real>* pos, R4<real>* pol, R2<real>* uv,
+                             int* ids, R2<real>* vel, int* cnt, int* key, int* count, int N, int* status,
+                             const int* flag) {
+    const int sl = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sl >= N || flag[0]) return;
+    const int id = slot_ids[sl];
+    const int i = reps[(unsigned)id >> local_bits].off + (int)((unsigned)id & ((1u << local_bits) - 1u));
     const real u = (real)i_uv[2 * i], v = (real)i_uv[2 * i + 1];
     int f = has_face ? i_face[i] : -1;
     if (f < 0) {
@@ -1173,7 +1176,6 @@ __global__ void k_load_state(const I* i_uv, const I* i_th, const int* i_face, co
     R2<real> U;
     U.x = u, U.y = v;
     uv[sl] = U;
-    const int id = packed_ids[i];
     ids[sl] = id;
     R2<real> Z;
     Z.x = 0, Z.y = 0;

@@ -427,6 +427,7 @@ def ensemble_leg(tg, steps=50, sample=64, autotune=False, replicas=4096):
             "interleaved_one_by_one": {"value": interleaved, "steps": 8,
                                        "path": "the same handles, one step of each replica in turn"},
             "batched_over_one_by_one": batched / one_by_one,
+            "batched_over_concurrent_streams": batched / concurrent,
             "roofline": {"bound": "hbm", "achieved": alg / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": alg / (k_ms * 1e-3) / 1e9 / peak, "traffic": None, "peak_source": peak_kind,
                          "kernel": "k_step", "kernel_ms": k_ms, "algorithmic_bytes": alg},

@@ -91,3 +91,39 @@ def test_lanes_need_128_thread_blocks(tg, mesh_l4):
     with pytest.raises(tg.TdsError):
         tg.Simulation(mesh_l4, tg.Params(), 100, tuning=dict(cells_per_particle=4.0, step_block=128, graph_steps=0,
                                                             lanes_per_particle=3))
+
+
+def test_autotune_ranks_the_candidates(tg):
+    """On a dense 200,000-particle system the candidates differ by up to 2x (4 lanes per particle run
+    the particle update four times over): the tuner must not pick a slow one, and its pick must run
+    at least about as fast as the default tuning timed here the same way."""
+    torch = pytest.importorskip("torch")
+    mesh = tg.Mesh.ellipsoid(4, (6.0, 3.0, 3.0))
+    n = 200000
+    R = float(np.sqrt(0.5 * mesh.area / (np.pi * n)))
+    p = tg.Params(radius=R, r_max=2.4 * R, eta=0.3, dt=0.01)
+    t, rate = tg.autotune(mesh, p, n, trial_steps=64)
+    assert t["lanes_per_particle"] == 1
+
+    def timed(tuning):
+        sim = tg.Simulation(mesh, p, n, seed=0, tuning=tuning)
+        sim.start()
+        sim.step(16)
+        stream = torch.cuda.ExternalStream(sim.stream())
+        best = None
+        for _ in range(2):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record(stream)
+            sim.step_async(64)
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        sim.close()
+        return n * 64 / (best * 1e-3)
+
+    default = timed(dict(cells_per_particle=4.0, step_block=128, graph_steps=0, lanes_per_particle=1))
+    slow = timed(dict(cells_per_particle=4.0, step_block=128, graph_steps=0, lanes_per_particle=4))
+    assert slow < 0.8 * default  # the candidates do differ
+    assert timed(t) > 0.9 * default
