@@ -666,7 +666,11 @@ def run_gpu(args):
                             "d2h_bytes_per_step": d_d2h, "synchronous": world * n * e2e_steps / d_sync_s,
                             "path": "the same loop through tds_set_state_async / tds_get_state_async (double "
                                     "arrays, the reference's type)"}}
+    # the step kernels, plus the loop graph's own: k_loop_set and k_loop_arm once per run, k_loop_ctl
+    # once per pass of each WHILE loop (blocks of 16 steps, then single steps)
     launches = sim.kernels_per_step() * args.steps
+    if args.steps >= 2 and sim.tuning()["graph_steps"] == 0:
+        launches += 2 + args.steps // 16 + args.steps % 16
     final = sim.get_state()
     sim.close()
 
