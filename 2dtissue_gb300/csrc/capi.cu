@@ -563,6 +563,7 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
         const RepParams<real>& r0 = *(const RepParams<real>*)s->reps_host.data();
         a.pc0.r_max2 = r0.r_max2, a.pc0.twoR = r0.twoR, a.pc0.inv_twoR = r0.inv_twoR, a.pc0.k = r0.k;
         a.pc0.adh_scale = r0.adh_scale;
+        a.rp0 = r0;
     }
     {
         KernelTimer kt(s, 3);
@@ -573,6 +574,8 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
             tdsk::k_step<real, 128, false, 2><<<(unsigned)((lanes + 127) / 128), 128, 0, st>>>(a);
         else if (s->lanes == 4)
             tdsk::k_step<real, 128, false, 4><<<(unsigned)((lanes + 127) / 128), 128, 0, st>>>(a);
+        else if (s->step_block == 128 && s->R == 1)
+            tdsk::k_step<real, 128, false, 1, true><<<(s->N + 127) / 128, 128, 0, st>>>(a);
         else if (s->step_block == 128)
             tdsk::k_step<real, 128><<<(s->N + 127) / 128, 128, 0, st>>>(a);
         else
