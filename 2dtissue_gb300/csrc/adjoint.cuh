@@ -51,8 +51,8 @@ struct AdjArgs {
     unsigned long long seed;
     const real* noise;  // injected noise of step t by global index, or null
     // loss terms of step t
-    const double* phisum;    // [R][6] order-parameter sums of step t (null: no order-parameter term)
-    const double* phibar;    // [R] dL/dphi_t
+    const R4<real>* phib;    // [R] the order-parameter adjoint of step t per replica: (dL/dS, S != 0),
+                             // S the step's sum of normalize((r' - c) x v) (null: no order-parameter term)
     const double* r_target;  // [3N] by global index, last step only (null otherwise)
     double w_pos;
     // adjoint state
@@ -61,7 +61,7 @@ struct AdjArgs {
     R4<real>* aF;        // [N] by slot: (Fbar, ubar_direct.x)
     R4<real>* aM;        // [N] by slot: (mbar, ubar_direct.y)
     R4<real>* aP;        // [N] by slot: (pbar_direct, 0)
-    double* gpar;        // [N][kGPar] by global index
+    real* gpar;          // [N][kGPar] by global index, in the working precision
     int N;
 };
 
@@ -211,17 +211,15 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 3 : 2)) k_ad
         const real s = (real)(2.0 * a.w_pos) * (real)rp.inv_n;
         for (int k = 0; k < 3; ++k) rb2[k] += s * (r2[k] - (real)a.r_target[3 * (size_t)gid + k]);
     }
-    if (a.phisum) {
-        // phi = |S| / N_r with S = sum_i normalize((r2_i - c) x v_i)
-        const double S0 = a.phisum[rep * 6], S1 = a.phisum[rep * 6 + 1], S2 = a.phisum[rep * 6 + 2];
-        const double Sn = sqrt(S0 * S0 + S1 * S1 + S2 * S2);
+    if (a.phib) {
+        // phi = |S| / N_r with S = sum_i normalize((r2_i - c) x v_i); dL/dS per replica (k_adj_phib)
+        const R4<real> sb = a.phib[rep];
         const real rc3[3] = {r2[0] - a.cx, r2[1] - a.cy, r2[2] - a.cz};
         real L[3];
         cross(rc3, v, L);
         const real Ln2 = dot(L, L);
-        if (Sn > 0 && Ln2 > (real)0) {
-            const double c = a.phibar[rep] * rp.inv_n / Sn;
-            const real Sb[3] = {(real)(c * S0), (real)(c * S1), (real)(c * S2)};
+        if (sb.w > (real)0 && Ln2 > (real)0) {
+            const real Sb[3] = {sb.x, sb.y, sb.z};
             const real iL = d_rsqrt(Ln2);
             const real ell[3] = {L[0] * iL, L[1] * iL, L[2] * iL};
             const real se = dot(Sb, ell);
@@ -255,8 +253,9 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 3 : 2)) k_ad
     for (int k = 0; k < 3; ++k) pb[k] = cd * p2b[k] + sd * p2bxn[k];
     // delta = dt omega + eta (u - 1/2)
     const real omegab = rp.dt * deltab;
-    double gv0 = 0, gmu = 0, gtau = 0, galign = 0, geta = 0;
-    if (!a.noise) geta = (double)(deltab * (u01 - (real)0.5));
+    // parameter terms in the working precision (GB300 runs FP64 at a small fraction of the FP32 rate)
+    real gv0 = 0, gmu = 0, gtau = 0, galign = 0, geta = 0;
+    if (!a.noise) geta = deltab * (u01 - (real)0.5);
     real mb[3] = {0, 0, 0};
     real nxp[3];
     cross(n, p, nxp);
@@ -264,7 +263,7 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 3 : 2)) k_ad
         // omega_1 = A1 / (|v| tau), A1 = p . (v x n)
         const real A1b = omegab * ivn * rp.inv_tau;
         const real vnb = -A1 * ivn * ivn * rp.inv_tau * omegab;
-        gtau += (double)(-A1 * ivn * rp.inv_tau * rp.inv_tau * omegab);
+        gtau += -A1 * ivn * rp.inv_tau * rp.inv_tau * omegab;
         real vxn[3];
         cross(v, n, vxn);
         for (int k = 0; k < 3; ++k) pb[k] += A1b * vxn[k], vb[k] += A1b * nxp[k] + vnb * v[k] * ivn;
@@ -273,7 +272,7 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 3 : 2)) k_ad
         // omega_2 = align B1 / |m|, B1 = p . (m x n)
         const real B1b = rp.align * omegab * imn;
         const real mnb = -rp.align * B1 * imn * imn * omegab;
-        galign += (double)(B1 * imn * omegab);
+        galign += B1 * imn * omegab;
         real mxn[3];
         cross(m, n, mxn);
         for (int k = 0; k < 3; ++k) pb[k] += B1b * mxn[k], mb[k] += B1b * nxp[k] + mnb * m[k] * imn;
@@ -281,13 +280,13 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 3 : 2)) k_ad
     real FTb[3];
     if (rp.force_mode == 0) {
         // v = v0 p + mu FT
-        gv0 += (double)dot(vb, p);
-        gmu += (double)dot(vb, FT);
+        gv0 += dot(vb, p);
+        gmu += dot(vb, FT);
         for (int k = 0; k < 3; ++k) pb[k] += rp.v0 * vb[k], FTb[k] = rp.mu * vb[k];
     } else {
         // v = (v0 + |FT|) p
         const real spb = dot(vb, p);
-        gv0 += (double)spb;
+        gv0 += spb;
         const real s = FTn > (real)0 ? spb / FTn : (real)0;
         for (int k = 0; k < 3; ++k) pb[k] += sp * vb[k], FTb[k] = s * FT[k];
     }
@@ -300,7 +299,7 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 3 : 2)) k_ad
     a.aF[q] = oF;
     a.aM[q] = oM;
     a.aP[q] = oP;
-    double* gp = a.gpar + (size_t)gid * kGPar;
+    real* gp = a.gpar + (size_t)gid * kGPar;
     gp[G_V0] += gv0;
     gp[G_MU] += gmu;
     gp[G_TAU] += gtau;
@@ -374,18 +373,39 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 5 : 3)) k_ad
     a.lam_out[3 * (size_t)gid] = ubx;
     a.lam_out[3 * (size_t)gid + 1] = uby;
     a.lam_out[3 * (size_t)gid + 2] = -sn * cb0 + cs * cb1;
-    double* gp = a.gpar + (size_t)gid * kGPar;
-    gp[G_KREP] += (double)gk;
-    gp[G_KADH] += (double)gkadh;
+    real* gp = a.gpar + (size_t)gid * kGPar;
+    gp[G_KREP] += gk;
+    gp[G_KADH] += gkadh;
+}
+
+// dL/dS of every stored step and replica, once per adjoint run: phi_t = |S_t| / N_r gives
+// dL/dS = phibar_t / (N_r |S_t|) S_t (the FP64 square root and division once per replica and step,
+// not once per particle); w = 1 when S_t != 0.
+template <typename real>
+__global__ void k_adj_phib(const double* phisum, const double* phibar, const RepParams<real>* reps, int R,
+                           long long TR, R4<real>* out) {
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= TR) return;
+    const int r = (int)(e % R);
+    const double S0 = phisum[e * 6], S1 = phisum[e * 6 + 1], S2 = phisum[e * 6 + 2];
+    const double Sn = sqrt(S0 * S0 + S1 * S1 + S2 * S2);
+    R4<real> o;
+    o.x = o.y = o.z = o.w = (real)0;
+    if (Sn > 0) {
+        const double c = phibar[e] * reps[r].inv_n / Sn;
+        o.x = (real)(c * S0), o.y = (real)(c * S1), o.z = (real)(c * S2), o.w = (real)1;
+    }
+    out[e] = o;
 }
 
 // Per-replica sums of the per-particle parameter terms, in a fixed order (one block per replica).
-__global__ void k_adj_reduce(const double* gpar, const int* off, const int* cnt, double* out) {
+template <typename real>
+__global__ void k_adj_reduce(const real* gpar, const int* off, const int* cnt, double* out) {
     __shared__ double s[256][kGPar];
     const int r = blockIdx.x;
     double acc[kGPar] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int i = off[r] + threadIdx.x; i < off[r] + cnt[r]; i += 256)
-        for (int k = 0; k < kGPar; ++k) acc[k] += gpar[(size_t)i * kGPar + k];
+        for (int k = 0; k < kGPar; ++k) acc[k] += (double)gpar[(size_t)i * kGPar + k];
     for (int k = 0; k < kGPar; ++k) s[threadIdx.x][k] = acc[k];
     __syncthreads();
     for (int w = 128; w > 0; w >>= 1) {

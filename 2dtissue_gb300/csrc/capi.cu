@@ -1068,8 +1068,8 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     const size_t b_state = N * (2 * sizeof(R4<real>) + sizeof(R2<real>) + 2 * sizeof(int));
     const size_t b_store = b_state + (M + 1) * sizeof(int);
     const size_t b_snap = b_state + M * sizeof(int) + 2 * (size_t)s->n_tiles * sizeof(int) + 64;
-    const size_t b_fixed = 2 * 3 * N * sizeof(real) + 3 * N * sizeof(R4<real>) + N * tdsk::kGPar * sizeof(double) +
-                           (size_t)T * R * 7 * sizeof(double) + 3 * N * sizeof(double) + b_snap;
+    const size_t b_fixed = 2 * 3 * N * sizeof(real) + 3 * N * sizeof(R4<real>) + N * tdsk::kGPar * sizeof(real) +
+                           (size_t)T * R * (7 * sizeof(double) + sizeof(R4<real>)) + 3 * N * sizeof(double) + b_snap;
     // checkpoint stride: the largest that fits (one stored segment + the checkpoints)
     int K = sp->checkpoint_stride;
     if (K <= 0) {
@@ -1094,7 +1094,9 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     std::vector<StepStore> store(K);
     real* lam[2] = {nullptr, nullptr};
     R4<real>*aF = nullptr, *aM = nullptr, *aP = nullptr;
-    double *gpar = nullptr, *phisum = nullptr, *phibar = nullptr, *rtgt = nullptr, *d_gp = nullptr;
+    real* gpar = nullptr;
+    R4<real>* dSb = nullptr;  // dL/dS per stored step and replica (k_adj_phib)
+    double *phisum = nullptr, *phibar = nullptr, *rtgt = nullptr, *d_gp = nullptr;
     int *d_off = nullptr, *d_cnt = nullptr;
     // all work buffers come from one block: measured first, then carved
     auto carve = [&](Carve& A) -> bool {
@@ -1108,13 +1110,14 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
         }
         lam[0] = A.get<real>(3 * N), lam[1] = A.get<real>(3 * N);
         aF = A.get<R4<real>>(N), aM = A.get<R4<real>>(N), aP = A.get<R4<real>>(N);
-        gpar = A.get<double>(N * tdsk::kGPar);
+        gpar = A.get<real>(N * tdsk::kGPar);
         phisum = A.get<double>((size_t)T * R * 6);
         phibar = A.get<double>((size_t)T * R);
+        dSb = A.get<R4<real>>((size_t)T * R);
         rtgt = sp->r3d_target ? A.get<double>(3 * N) : nullptr;
         d_off = A.get<int>(R), d_cnt = A.get<int>(R);
         d_gp = A.get<double>(R * tdsk::kGPar);
-        return ok && lam[0] && lam[1] && aF && aM && aP && gpar && phisum && phibar && d_off && d_cnt && d_gp &&
+        return ok && lam[0] && lam[1] && aF && aM && aP && gpar && phisum && phibar && dSb && d_off && d_cnt && d_gp &&
                (!sp->r3d_target || rtgt);
     };
     {
@@ -1214,7 +1217,10 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     // ---- reverse sweep ----
     Range rev("adjoint reverse");
     CK(cudaMemsetAsync(lam[0], 0, 3 * N * sizeof(real), s->stream));
-    CK(cudaMemsetAsync(gpar, 0, N * tdsk::kGPar * sizeof(double), s->stream));
+    CK(cudaMemsetAsync(gpar, 0, N * tdsk::kGPar * sizeof(real), s->stream));
+    if (phi_term)
+        tdsk::k_adj_phib<real><<<(unsigned)(((long long)T * R + 255) / 256), 256, 0, s->stream>>>(
+            phisum, phibar, (const RepParams<real>*)s->reps, (int)R, (long long)T * R, dSb);
     int cur = 0;
     tdsk::AdjArgs<real> a;
     std::memset(&a, 0, sizeof a);
@@ -1245,8 +1251,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
             a.pos = (const R4<real>*)x.pos, a.pol = (const R4<real>*)x.pol, a.uv = (const R2<real>*)x.uv;
             a.ids = x.ids, a.key = x.key, a.start = x.start;
             a.step = t_base + t;
-            a.phisum = phi_term ? phisum + (size_t)t * R * 6 : nullptr;
-            a.phibar = phi_term ? phibar + (size_t)t * R : nullptr;
+            a.phib = phi_term ? dSb + (size_t)t * R : nullptr;
             a.r_target = (t == T - 1 && rtgt && sp->w_pos > 0) ? rtgt : nullptr;
             a.lam_in = lam[cur];
             a.lam_out = lam[cur ^ 1];
@@ -1255,7 +1260,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
             cur ^= 1;
         }
     }
-    tdsk::k_adj_reduce<<<(int)R, 256, 0, s->stream>>>(gpar, d_off, d_cnt, d_gp);
+    tdsk::k_adj_reduce<real><<<(int)R, 256, 0, s->stream>>>(gpar, d_off, d_cnt, d_gp);
     CK(cudaGetLastError());
     snapshot_copy<real>(s, fin, false);  // the handle ends where the forward ended
     std::vector<real> lh(3 * N);
