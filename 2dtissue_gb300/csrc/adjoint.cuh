@@ -24,9 +24,10 @@ namespace tdsk {
 
 enum : int { G_KREP = 0, G_KADH = 1, G_V0 = 2, G_MU = 3, G_TAU = 4, G_ALIGN = 5, G_ETA = 6, kGPar = 8 };
 // Block of k_adj_a / k_adj_b. Their candidate-run tables are shared-memory columns (entry r of
-// thread t at run[r * kAdjThreads]) rather than stack arrays, and the register limits (3 blocks
-// per SM for k_adj_a, 5 for k_adj_b in FP32) trade a few spills for occupancy: together 3.51 ->
-// 3.15 ms per reverse step on the 512-replica bumpy-sphere ensemble.
+// thread t at run[r * kAdjThreads]) rather than stack arrays, and the register limits (4 blocks
+// per SM for k_adj_a, 5 for k_adj_b in FP32) trade a few spills for occupancy (k_adj_a at 4 rather
+// than 3 blocks: forward+adjoint 2.48e9 -> 2.61e9 particle-steps/s on the 512-replica bumpy-sphere
+// ensemble).
 constexpr int kAdjThreads = 256;
 
 template <typename real>
@@ -122,7 +123,7 @@ __device__ __forceinline__ real dot(const real a[3], const real b[3]) {
 }
 
 template <typename real>
-__global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 3 : 2)) k_adj_a(const AdjArgs<real> a) {
+__global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 4 : 2)) k_adj_a(const AdjArgs<real> a) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= a.N) return;
     const R4<real> P = a.pos[q];
