@@ -39,6 +39,8 @@ struct AdjArgs {
     const int* ids;
     const int* key;
     const int* start;
+    const R4<real>* sum_f;  // step t's pair sums by slot (F, m.x), (m.y, m.z), or null (recomputed)
+    const R2<real>* sum_m;
     const uint4* desc;
     const real* rec;
     const int4* adj;
@@ -138,13 +140,20 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 4 : 2)) k_ad
     const real* g = a.rec + (size_t)f * kRec;
 
     // ---- forward recompute (the arithmetic of k_step) ----
-    __shared__ int2 s_run[9 * kAdjThreads];
-    int2* run = s_run + threadIdx.x;
-    const int total = candidate_runs(rp, a.desc, a.start, a.key[q], run);
     real acc[6] = {0, 0, 0, 0, 0, 0};
-    int cnt = 0;
-    // the step kernel's own pair loop (same visiting order and arithmetic: the same sums, bit for bit)
-    pair_sums_s<real, kAdjThreads>(pair_constants(rp), P, a.pos, a.pol, run, total, q, acc, cnt);
+    if (a.sum_f) {
+        // the pair sums the forward step stored (the step kernel's own values)
+        const R4<real> sf = a.sum_f[q];
+        const R2<real> sm = a.sum_m[q];
+        acc[0] = sf.x, acc[1] = sf.y, acc[2] = sf.z, acc[3] = sf.w, acc[4] = sm.x, acc[5] = sm.y;
+    } else {
+        __shared__ int2 s_run[9 * kAdjThreads];
+        int2* run = s_run + threadIdx.x;
+        const int total = candidate_runs(rp, a.desc, a.start, a.key[q], run);
+        int cnt = 0;
+        // the step kernel's own pair loop (same visiting order and arithmetic: the same sums, bit for bit)
+        pair_sums_s<real, kAdjThreads>(pair_constants(rp), P, a.pos, a.pol, run, total, q, acc, cnt);
+    }
     const real p[3] = {PL.x, PL.y, PL.z};
     const real F[3] = {acc[0], acc[1], acc[2]};
     const real m[3] = {acc[3], acc[4], acc[5]};

@@ -456,6 +456,8 @@ struct StepStore {
     int* ids = nullptr;
     int* key = nullptr;
     int* start = nullptr;
+    void* sum_f = nullptr;  // the step's pair sums by slot (null: the reverse step recomputes them)
+    void* sum_m = nullptr;
 };
 struct StepHooks {
     const StepStore* store = nullptr;
@@ -559,6 +561,8 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
     a.single = s->R == 1;
     a.nbr_list = nbr_list;
     a.nbr_cap = nbr_cap;
+    a.sum_f = x ? (R4<real>*)x->sum_f : nullptr;
+    a.sum_m = x ? (R2<real>*)x->sum_m : nullptr;
     {
         const RepParams<real>& r0 = *(const RepParams<real>*)s->reps_host.data();
         a.pc0.r_max2 = r0.r_max2, a.pc0.twoR = r0.twoR, a.pc0.inv_twoR = r0.inv_twoR, a.pc0.k = r0.k;
@@ -568,7 +572,11 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
     {
         KernelTimer kt(s, 3);
         const long long lanes = (long long)s->N * s->lanes;
-        if (nbr_list)
+        if (a.sum_f && s->R == 1)  // a stored step of the adjoint (one lane per particle): bit-identical
+            tdsk::k_step<real, 128, false, 1, true, true><<<(s->N + 127) / 128, 128, 0, st>>>(a);
+        else if (a.sum_f)
+            tdsk::k_step<real, 128, false, 1, false, true><<<(s->N + 127) / 128, 128, 0, st>>>(a);
+        else if (nbr_list)
             tdsk::k_step<real, 128, true><<<(s->N + 127) / 128, 128, 0, st>>>(a);
         else if (s->lanes == 2)
             tdsk::k_step<real, 128, false, 2><<<(unsigned)((lanes + 127) / 128), 128, 0, st>>>(a);
@@ -1066,7 +1074,10 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     const int T = sp->n_steps;
     const size_t N = (size_t)s->N, M = (size_t)s->M, R = (size_t)s->R;
     const size_t b_state = N * (2 * sizeof(R4<real>) + sizeof(R2<real>) + 2 * sizeof(int));
-    const size_t b_store = b_state + (M + 1) * sizeof(int);
+    // the stored steps keep their pair sums (24 B per particle in FP32) when the step kernel runs one
+    // lane per particle (with more lanes its sums round differently from the reverse step's loop)
+    const bool keep_sums = s->lanes == 1;
+    const size_t b_store = b_state + (M + 1) * sizeof(int) + (keep_sums ? N * (sizeof(R4<real>) + sizeof(R2<real>)) : 0);
     const size_t b_snap = b_state + M * sizeof(int) + 2 * (size_t)s->n_tiles * sizeof(int) + 64;
     const size_t b_fixed = 2 * 3 * N * sizeof(real) + 3 * N * sizeof(R4<real>) + N * tdsk::kGPar * sizeof(real) +
                            (size_t)T * R * (7 * sizeof(double) + sizeof(R4<real>)) + 3 * N * sizeof(double) + b_snap;
@@ -1107,6 +1118,10 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
             x.pos = A.get<R4<real>>(N), x.pol = A.get<R4<real>>(N), x.uv = A.get<R2<real>>(N);
             x.ids = A.get<int>(N), x.key = A.get<int>(N), x.start = A.get<int>(M + 1);
             ok = ok && x.pos && x.pol && x.uv && x.ids && x.key && x.start;
+            if (keep_sums) {
+                x.sum_f = A.get<R4<real>>(N), x.sum_m = A.get<R2<real>>(N);
+                ok = ok && x.sum_f && x.sum_m;
+            }
         }
         lam[0] = A.get<real>(3 * N), lam[1] = A.get<real>(3 * N);
         aF = A.get<R4<real>>(N), aM = A.get<R4<real>>(N), aP = A.get<R4<real>>(N);
@@ -1250,6 +1265,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
             const StepStore& x = store[t - t0];
             a.pos = (const R4<real>*)x.pos, a.pol = (const R4<real>*)x.pol, a.uv = (const R2<real>*)x.uv;
             a.ids = x.ids, a.key = x.key, a.start = x.start;
+            a.sum_f = (const R4<real>*)x.sum_f, a.sum_m = (const R2<real>*)x.sum_m;
             a.step = t_base + t;
             a.phib = phi_term ? dSb + (size_t)t * R : nullptr;
             a.r_target = (t == T - 1 && rtgt && sp->w_pos > 0) ? rtgt : nullptr;

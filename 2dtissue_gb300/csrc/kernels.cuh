@@ -126,6 +126,8 @@ struct StepArgs {
     RepParams<real> rp0;  // the replica's parameters when there is one (read from the constant bank)
     int* nbr_list;  // neighbour export (the NBR instantiation only): nbr_cap ids per particle
     int nbr_cap;
+    R4<real>* sum_f;  // the pair sums by slot (the STORE instantiation only): (F, m.x)
+    R2<real>* sum_m;  //   and (m.y, m.z), for the adjoint's reverse step
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -587,7 +589,10 @@ __device__ __forceinline__ void pair_sums_lanes(const PairC<real>& pc, const R4<
 // SINGLE: a one-replica system reads its parameters from the kernel arguments (rp0, the constant
 // bank: operands of the arithmetic, no loads) instead of the replica table (2.2% faster at 1M
 // particles, results bit-identical).
-template <typename real, int BLOCK, bool NBR = false, int LPP = 1, bool SINGLE = false>
+// STORE: a step whose sorted state the adjoint keeps also stores its pair sums (force F and
+// neighbour polarity sum m, by slot), so that the reverse step reads them instead of running the
+// pair loop again.
+template <typename real, int BLOCK, bool NBR = false, int LPP = 1, bool SINGLE = false, bool STORE = false>
 __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLOCK) k_step(const StepArgs<real> a) {
     typedef R4<real> r4;
     static_assert(LPP == 1 || LPP == 2 || LPP == 4, "1, 2 or 4 lanes per particle");
@@ -657,6 +662,14 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
                 for (int k = 0; k < 6; ++k) acc[k] += __shfl_xor_sync(gm, acc[k], o);
                 cnt += __shfl_xor_sync(gm, cnt, o);
             }
+        }
+        if (STORE) {
+            R4<real> sf;
+            sf.x = acc[0], sf.y = acc[1], sf.z = acc[2], sf.w = acc[3];
+            R2<real> sm;
+            sm.x = acc[4], sm.y = acc[5];
+            a.sum_f[q] = sf;
+            a.sum_m[q] = sm;
         }
         }
         // the rest of the particle's own state, read again (an L1/L2 hit) rather than kept live
