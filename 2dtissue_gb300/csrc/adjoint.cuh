@@ -124,8 +124,11 @@ __device__ __forceinline__ real dot(const real a[3], const real b[3]) {
     return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
 }
 
-template <typename real>
-__global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 4 : 2)) k_adj_a(const AdjArgs<real> a) {
+// STORED: the forward stored this step's pair sums (a.sum_f, a.sum_m), so the kernel has no pair
+// loop and fewer registers; otherwise the sums are recomputed with the step kernel's own loop.
+template <typename real, bool STORED>
+__global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? (STORED ? 6 : 4) : 2))
+    k_adj_a(const AdjArgs<real> a) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= a.N) return;
     const R4<real> P = a.pos[q];
@@ -141,7 +144,7 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 4 : 2)) k_ad
 
     // ---- forward recompute (the arithmetic of k_step) ----
     real acc[6] = {0, 0, 0, 0, 0, 0};
-    if (a.sum_f) {
+    if (STORED) {
         // the pair sums the forward step stored (the step kernel's own values)
         const R4<real> sf = a.sum_f[q];
         const R2<real> sm = a.sum_m[q];

@@ -1271,7 +1271,12 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
             a.r_target = (t == T - 1 && rtgt && sp->w_pos > 0) ? rtgt : nullptr;
             a.lam_in = lam[cur];
             a.lam_out = lam[cur ^ 1];
-            tdsk::k_adj_a<real><<<(s->N + tdsk::kAdjThreads - 1) / tdsk::kAdjThreads, tdsk::kAdjThreads, 0, s->stream>>>(a);
+            if (a.sum_f)
+                tdsk::k_adj_a<real, true><<<(s->N + tdsk::kAdjThreads - 1) / tdsk::kAdjThreads, tdsk::kAdjThreads, 0,
+                                            s->stream>>>(a);
+            else
+                tdsk::k_adj_a<real, false><<<(s->N + tdsk::kAdjThreads - 1) / tdsk::kAdjThreads, tdsk::kAdjThreads, 0,
+                                             s->stream>>>(a);
             tdsk::k_adj_b<real><<<(s->N + tdsk::kAdjThreads - 1) / tdsk::kAdjThreads, tdsk::kAdjThreads, 0, s->stream>>>(a);
             cur ^= 1;
         }
