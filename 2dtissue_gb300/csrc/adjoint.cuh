@@ -6,7 +6,8 @@
 // so the adjoint state is (ubar, vbar, thetabar) per particle, indexed by global particle index.
 //
 // One reverse step of step t is two launches over step t's sorted state:
-//   k_adj_a  per particle: recomputes the forward update (pair sums, velocity, polarity rotation,
+//   k_adj_a  per particle: recomputes the forward update (pair sums -- read from the forward's
+//            store, or recomputed with the step kernel's loop --, velocity, polarity rotation,
 //            chart advance, seam wrap, location, map) and runs its reverse from the adjoint of the
 //            state after the step (plus the loss terms on the new positions and the order
 //            parameter) down to the adjoints of the pair sums F (force) and m (neighbour polarity)
@@ -94,23 +95,6 @@ __device__ __forceinline__ int candidate_runs(const RepParams<real>& rp, const u
         }
     }
     return total;
-}
-
-// Visits the candidates in the forward step's order (runs 0..8, slots ascending).
-template <typename F>
-__device__ __forceinline__ void for_candidates(const int2* run, int total, F&& fn) {
-    int2 x0 = run[0];
-    int r = 0, t = x0.x, left = x0.y;
-    for (int k = 0; k < total; ++k) {
-        while (left == 0) {
-            const int2 x = run[(++r) * kAdjThreads];
-            t = x.x;
-            left = x.y;
-        }
-        fn(t);
-        ++t;
-        --left;
-    }
 }
 
 template <typename real>
@@ -341,32 +325,61 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 5 : 3)) k_ad
     real rb[3] = {0, 0, 0}, msum[3] = {0, 0, 0};
     real gk = 0, gkadh = 0;  // the particle's few pair terms, summed in the working precision
     const real inv_w = rp.inv_adh_w;
-    for_candidates(run, total, [&](int t) {
-        const R4<real> Q = a.pos[t];
+    // one neighbour's terms (candidate order, as the forward adds them)
+    auto nbr_term = [&](int t, const R4<real>& Q) {
         const real dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
-        const real d2 = pair_d2(P, Q);  // the forward's neighbour test, rounded the same way
-        if (d2 < rp.r_max2 && t != q) {
-            const R4<real> Fj = a.aF[t], Mj = a.aM[t];
-            msum[0] += Mj.x, msum[1] += Mj.y, msum[2] += Mj.z;
-            if (d2 > (real)0) {
-                const real rd = d_rsqrt(d2);
-                const real d = d2 * rd;
-                const bool rep_branch = d < rp.twoR;
-                const real fm = rep_branch ? rp.k * (rp.twoR - d) * rp.inv_twoR : -(rp.adh_scale * (d - rp.twoR));
-                const real fp = rep_branch ? -rp.k * rp.inv_twoR : -rp.adh_scale;
-                const real e[3] = {dx * rd, dy * rd, dz * rd};
-                const real D[3] = {myF.x - Fj.x, myF.y - Fj.y, myF.z - Fj.z};
-                const real eD = dot(e, D);
-                const real fd = fm * rd;
-                for (int k = 0; k < 3; ++k) rb[k] += fd * D[k] + (fp - fd) * eD * e[k];
-                const real Fe = myF.x * e[0] + myF.y * e[1] + myF.z * e[2];
-                if (rep_branch)
-                    gk += Fe * (rp.twoR - d) * rp.inv_twoR;
-                else
-                    gkadh += -Fe * (d - rp.twoR) * inv_w;
-            }
+        const real d2 = pair_d2(P, Q);
+        const R4<real> Fj = a.aF[t], Mj = a.aM[t];
+        msum[0] += Mj.x, msum[1] += Mj.y, msum[2] += Mj.z;
+        if (d2 > (real)0) {
+            const real rd = d_rsqrt(d2);
+            const real d = d2 * rd;
+            const bool rep_branch = d < rp.twoR;
+            const real fm = rep_branch ? rp.k * (rp.twoR - d) * rp.inv_twoR : -(rp.adh_scale * (d - rp.twoR));
+            const real fp = rep_branch ? -rp.k * rp.inv_twoR : -rp.adh_scale;
+            const real e[3] = {dx * rd, dy * rd, dz * rd};
+            const real D[3] = {myF.x - Fj.x, myF.y - Fj.y, myF.z - Fj.z};
+            const real eD = dot(e, D);
+            const real fd = fm * rd;
+            for (int k = 0; k < 3; ++k) rb[k] += fd * D[k] + (fp - fd) * eD * e[k];
+            const real Fe = myF.x * e[0] + myF.y * e[1] + myF.z * e[2];
+            if (rep_branch)
+                gk += Fe * (rp.twoR - d) * rp.inv_twoR;
+            else
+                gkadh += -Fe * (d - rp.twoR) * inv_w;
         }
-    });
+    };
+    // two candidates per iteration: both distance tests (the forward's neighbour test, rounded the
+    // same way) before either neighbour's terms
+    if (total > 0) {
+        const int2* sp = run;
+        int2 x0 = *sp;
+        int t = x0.x, left = x0.y;
+        for (int rem = total; rem > 0; rem -= 2) {
+            if (left == 0) {
+                sp += kAdjThreads;
+                const int2 x = *sp;
+                t = x.x, left = x.y;
+            }
+            const int ta = t++;
+            --left;
+            int tb = ta;
+            if (rem > 1) {
+                if (left == 0) {
+                    sp += kAdjThreads;
+                    const int2 x = *sp;
+                    t = x.x, left = x.y;
+                }
+                tb = t++;
+                --left;
+            }
+            const R4<real> Qa = a.pos[ta], Qb = a.pos[tb];
+            const bool na = pair_d2(P, Qa) < rp.r_max2 && ta != q;
+            const bool nb = rem > 1 && pair_d2(P, Qb) < rp.r_max2 && tb != q;
+            if (na) nbr_term(ta, Qa);
+            if (nb) nbr_term(tb, Qb);
+        }
+    }
     // r = A + J (uv - a)
     const R4<real> g2 = rq(g, 2), g3 = rq(g, 3);
     const real Ju[3] = {g2.x, g2.y, g2.z}, Jv[3] = {g2.w, g3.x, g3.y};
