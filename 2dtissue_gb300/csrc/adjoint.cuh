@@ -25,10 +25,10 @@ namespace tdsk {
 
 enum : int { G_KREP = 0, G_KADH = 1, G_V0 = 2, G_MU = 3, G_TAU = 4, G_ALIGN = 5, G_ETA = 6, kGPar = 8 };
 // Block of k_adj_a / k_adj_b. Their candidate-run tables are shared-memory columns (entry r of
-// thread t at run[r * kAdjThreads]) rather than stack arrays, and the register limits (4 blocks
-// per SM for k_adj_a, 5 for k_adj_b in FP32) trade a few spills for occupancy (k_adj_a at 4 rather
-// than 3 blocks: forward+adjoint 2.48e9 -> 2.61e9 particle-steps/s on the 512-replica bumpy-sphere
-// ensemble).
+// thread t at run[r * kAdjThreads]) rather than stack arrays, and the register limits trade a few
+// spills for occupancy (FP32: k_adj_a at 6 blocks per SM when it reads stored pair sums, 4 when it
+// runs the pair loop, k_adj_b at 5; k_adj_a at 4 rather than 3 blocks took forward+adjoint from
+// 2.48e9 to 2.61e9 particle-steps/s on the 512-replica bumpy-sphere ensemble).
 constexpr int kAdjThreads = 256;
 
 template <typename real>
@@ -110,42 +110,194 @@ __device__ __forceinline__ real dot(const real a[3], const real b[3]) {
 
 // STORED: the forward stored this step's pair sums (a.sum_f, a.sum_m), so the kernel has no pair
 // loop and fewer registers; otherwise the sums are recomputed with the step kernel's own loop.
+// Two phases, so that few values are live at any point: the forward recompute runs through the
+// step's discrete decisions (seam wraps, the new face) and the new position, whose adjoint terms
+// are taken at once; the reverse of the polarity and velocity update then recomputes what it
+// needs from the step's inputs, read again (L1/L2 hits), rather than keeping the forward's
+// intermediates live (or spilled) across the wrap and the location: FP32 spills 180/356 -> 60/52
+// bytes per thread at 6 blocks per SM (0/0 with the pair loop at 4), forward+adjoint +1.5% on the
+// 512-replica bumpy-sphere ensemble, the results unchanged.
 template <typename real, bool STORED>
 __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? (STORED ? 6 : 4) : 2))
     k_adj_a(const AdjArgs<real> a) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= a.N) return;
-    const R4<real> P = a.pos[q];
-    const R4<real> PL = a.pol[q];
-    const R2<real> U = a.uv[q];
-    const int id = a.ids[q];
-    const int rep = (int)((unsigned)id >> a.local_bits);
-    const unsigned local = (unsigned)id & ((1u << a.local_bits) - 1u);
-    const RepParams<real>& rp = a.reps[rep];
-    const int gid = rp.off + (int)local;
-    const int f = real_to_face(PL.w);
-    const real* g = a.rec + (size_t)f * kRec;
-
-    // ---- forward recompute (the arithmetic of k_step) ----
     real acc[6] = {0, 0, 0, 0, 0, 0};
-    if (STORED) {
-        // the pair sums the forward step stored (the step kernel's own values)
-        const R4<real> sf = a.sum_f[q];
-        const R2<real> sm = a.sum_m[q];
-        acc[0] = sf.x, acc[1] = sf.y, acc[2] = sf.z, acc[3] = sf.w, acc[4] = sm.x, acc[5] = sm.y;
-    } else {
-        __shared__ int2 s_run[9 * kAdjThreads];
-        int2* run = s_run + threadIdx.x;
-        const int total = candidate_runs(rp, a.desc, a.start, a.key[q], run);
-        int cnt = 0;
-        // the step kernel's own pair loop (same visiting order and arithmetic: the same sums, bit for bit)
-        pair_sums_s<real, kAdjThreads>(pair_constants(rp), P, a.pos, a.pol, run, total, q, acc, cnt);
+    real cd, sd, u01 = (real)0.5, ub2x, ub2y, thb2, vb[3] = {0, 0, 0};
+    {
+        const R4<real> PL = a.pol[q];
+        const R2<real> U = a.uv[q];
+        const int id = a.ids[q];
+        const int rep = (int)((unsigned)id >> a.local_bits);
+        const unsigned local = (unsigned)id & ((1u << a.local_bits) - 1u);
+        const RepParams<real>& rp = a.reps[rep];
+        const int gid = rp.off + (int)local;
+        const int f = real_to_face(PL.w);
+        const real* g = a.rec + (size_t)f * kRec;
+
+        // ---- forward recompute (the arithmetic of k_step) ----
+        if (STORED) {
+            // the pair sums the forward step stored (the step kernel's own values)
+            const R4<real> sf = a.sum_f[q];
+            const R2<real> sm = a.sum_m[q];
+            acc[0] = sf.x, acc[1] = sf.y, acc[2] = sf.z, acc[3] = sf.w, acc[4] = sm.x, acc[5] = sm.y;
+        } else {
+            __shared__ int2 s_run[9 * kAdjThreads];
+            int2* run = s_run + threadIdx.x;
+            const R4<real> P = a.pos[q];
+            const int total = candidate_runs(rp, a.desc, a.start, a.key[q], run);
+            int cnt = 0;
+            // the step kernel's own pair loop (same visiting order and arithmetic: the same sums, bit for bit)
+            pair_sums_s<real, kAdjThreads>(pair_constants(rp), P, a.pos, a.pol, run, total, q, acc, cnt);
+        }
+        const real p[3] = {PL.x, PL.y, PL.z};
+        const real F[3] = {acc[0], acc[1], acc[2]};
+        const real m[3] = {acc[3], acc[4], acc[5]};
+        real n[3], Jp[6];
+        face_frame(g, n, Jp);
+        const real Fn = dot(F, n);
+        const real FT[3] = {F[0] - Fn * n[0], F[1] - Fn * n[1], F[2] - Fn * n[2]};
+        real v[3];
+        if (rp.force_mode == 0) {
+            for (int k = 0; k < 3; ++k) v[k] = rp.v0 * p[k] + rp.mu * FT[k];
+        } else {
+            const real t2 = dot(FT, FT);
+            const real FTn = t2 > (real)0 ? t2 * d_rsqrt(t2) : (real)0;
+            const real sp = rp.v0 + FTn;
+            for (int k = 0; k < 3; ++k) v[k] = sp * p[k];
+        }
+        const real vn2 = dot(v, v), mn2 = dot(m, m);
+        const real ivn = vn2 > (real)0 ? d_rsqrt(vn2) : (real)0;
+        const real imn = mn2 > (real)0 ? d_rsqrt(mn2) : (real)0;
+        real pxv[3], pxm[3];
+        cross(p, v, pxv);
+        cross(p, m, pxm);
+        const real A1 = dot(pxv, n), B1 = dot(pxm, n);
+        const real omega = A1 * ivn * rp.inv_tau + rp.align * B1 * imn;
+        real xi;
+        if (a.noise) {
+            xi = a.noise[gid];
+        } else {
+            const unsigned bits = tdsr::noise_bits24(a.seed, a.step, local, (unsigned)rep);
+            u01 = (real)bits * (real)(1.0 / 16777216.0);
+            xi = rp.eta * (u01 - (real)0.5);
+        }
+        const real delta = rp.dt * omega + xi;
+        d_sincos(delta, &sd, &cd);
+        real np[3];
+        cross(n, p, np);
+        const real p2[3] = {cd * p[0] + sd * np[0], cd * p[1] + sd * np[1], cd * p[2] + sd * np[2]};
+        const real w0 = Jp[0] * p2[0] + Jp[1] * p2[1] + Jp[2] * p2[2];
+        const real w1 = Jp[3] * p2[0] + Jp[4] * p2[1] + Jp[5] * p2[2];
+        const real vu = Jp[0] * v[0] + Jp[1] * v[1] + Jp[2] * v[2];
+        const real vv = Jp[3] * v[0] + Jp[4] * v[1] + Jp[5] * v[2];
+        const real u2 = U.x + rp.dt * vu, v2 = U.y + rp.dt * vv;
+        real ex = u2, ey = v2, tvu = vu, tvv = vv, tw0 = w0, tw1 = w1;
+        int nw = 0;
+        seam_wrap(U.x, U.y, ex, ey, tvu, tvv, tw0, tw1, nw);
+        // linear part of the composed gluing maps: the same wrap applied to the unit vectors
+        real R00 = 1, R10 = 0, R01 = 0, R11 = 1;
+        if (nw > 0) {
+            real ex2 = u2, ey2 = v2;
+            int nw2 = 0;
+            seam_wrap(U.x, U.y, ex2, ey2, R00, R10, R01, R11, nw2);
+        }
+        int mode = 0;
+        const int f2 = locate(a.rec, a.adj, a.G, a.bin_start, a.bin_faces, ex, ey, f, mode);
+        const real* h = a.rec + (size_t)f2 * kRec;
+        real r2[3];
+        face_map(h, ex, ey, r2[0], r2[1], r2[2]);
+
+        // ---- reverse of the new position's terms ----
+        real ub3x = a.lam_in[3 * (size_t)gid], ub3y = a.lam_in[3 * (size_t)gid + 1];
+        thb2 = a.lam_in[3 * (size_t)gid + 2];
+        real rb2[3] = {0, 0, 0};
+        if (a.r_target) {
+            const real s = (real)(2.0 * a.w_pos) * (real)rp.inv_n;
+            for (int k = 0; k < 3; ++k) rb2[k] += s * (r2[k] - (real)a.r_target[3 * (size_t)gid + k]);
+        }
+        if (a.phib) {
+            // phi = |S| / N_r with S = sum_i normalize((r2_i - c) x v_i); dL/dS per replica (k_adj_phib)
+            const R4<real> sb = a.phib[rep];
+            const real rc3[3] = {r2[0] - a.cx, r2[1] - a.cy, r2[2] - a.cz};
+            real L[3];
+            cross(rc3, v, L);
+            const real Ln2 = dot(L, L);
+            if (sb.w > (real)0 && Ln2 > (real)0) {
+                const real Sb[3] = {sb.x, sb.y, sb.z};
+                const real iL = d_rsqrt(Ln2);
+                const real ell[3] = {L[0] * iL, L[1] * iL, L[2] * iL};
+                const real se = dot(Sb, ell);
+                const real Lb[3] = {(Sb[0] - se * ell[0]) * iL, (Sb[1] - se * ell[1]) * iL,
+                                    (Sb[2] - se * ell[2]) * iL};
+                real t1[3], t2[3];
+                cross(v, Lb, t1);    // rc3bar = v x Lbar
+                cross(Lb, rc3, t2);  // vbar  += Lbar x rc
+                for (int k = 0; k < 3; ++k) rb2[k] += t1[k], vb[k] += t2[k];
+            }
+        }
+        // r2 = A' + J' (uv3 - a')
+        const R4<real> h2 = rq(h, 2), h3 = rq(h, 3);
+        ub3x += h2.x * rb2[0] + h2.y * rb2[1] + h2.z * rb2[2];
+        ub3y += h2.w * rb2[0] + h3.x * rb2[1] + h3.y * rb2[2];
+        // uv3 = R uv2 + t
+        ub2x = R00 * ub3x + R10 * ub3y, ub2y = R01 * ub3x + R11 * ub3y;
     }
+
+    // ---- reverse of the polarity and velocity update, on values recomputed from the inputs ----
+    const R4<real> PL = reload(a.pol, q);
+    const int id = reload(a.ids, q);
+    const int rep = (int)((unsigned)id >> a.local_bits);
+    const RepParams<real>& rp = a.reps[rep];
+    const int gid = rp.off + (int)((unsigned)id & ((1u << a.local_bits) - 1u));
+    const real* g = a.rec + (size_t)real_to_face(PL.w) * kRec;
+    asm volatile("" : "+l"(g));
     const real p[3] = {PL.x, PL.y, PL.z};
-    const real F[3] = {acc[0], acc[1], acc[2]};
-    const real m[3] = {acc[3], acc[4], acc[5]};
-    real n[3], Jp[6];
-    face_frame(g, n, Jp);
+    real n[3];
+    real vbv[3], p2b[3];
+    {
+        real Jp[6];
+        face_frame(g, n, Jp);
+        real np[3];
+        cross(n, p, np);
+        const real p2[3] = {cd * p[0] + sd * np[0], cd * p[1] + sd * np[1], cd * p[2] + sd * np[2]};
+        const real w0 = Jp[0] * p2[0] + Jp[1] * p2[1] + Jp[2] * p2[2];
+        const real w1 = Jp[3] * p2[0] + Jp[4] * p2[1] + Jp[5] * p2[2];
+        // uv2 = uv + dt (Jp v)
+        const real velbx = rp.dt * ub2x, velby = rp.dt * ub2y;
+        for (int k = 0; k < 3; ++k) vbv[k] = Jp[k] * velbx + Jp[3 + k] * velby;
+        // theta2 = atan2(w1, w0) + const (the gluing rotations only add constants)
+        const real iw2 = (real)1 / (w0 * w0 + w1 * w1);
+        const real wb0 = -w1 * iw2 * thb2, wb1 = w0 * iw2 * thb2;
+        // w = Jp p2
+        for (int k = 0; k < 3; ++k) p2b[k] = Jp[k] * wb0 + Jp[3 + k] * wb1;
+    }
+    for (int k = 0; k < 3; ++k) vb[k] += vbv[k];
+    // p2 = cos(delta) p + sin(delta) (n x p)
+    real deltab, pb[3];
+    {
+        real np[3];
+        cross(n, p, np);
+        deltab = p2b[0] * (cd * np[0] - sd * p[0]) + p2b[1] * (cd * np[1] - sd * p[1]) +
+                 p2b[2] * (cd * np[2] - sd * p[2]);
+        real p2bxn[3];
+        cross(p2b, n, p2bxn);
+        for (int k = 0; k < 3; ++k) pb[k] = cd * p2b[k] + sd * p2bxn[k];
+    }
+    // delta = dt omega + eta (u - 1/2)
+    const real omegab = rp.dt * deltab;
+    // parameter terms in the working precision (GB300 runs FP64 at a small fraction of the FP32 rate)
+    real gv0 = 0, gmu = 0, gtau = 0, galign = 0, geta = 0;
+    if (!a.noise) geta = deltab * (u01 - (real)0.5);
+    // the pair sums again: stored (read again) or kept from the forward recompute
+    real F[3], m[3];
+    if (STORED) {
+        const R4<real> sf = reload(a.sum_f, q);
+        const R2<real> sm = reload(a.sum_m, q);
+        F[0] = sf.x, F[1] = sf.y, F[2] = sf.z, m[0] = sf.w, m[1] = sm.x, m[2] = sm.y;
+    } else {
+        F[0] = acc[0], F[1] = acc[1], F[2] = acc[2], m[0] = acc[3], m[1] = acc[4], m[2] = acc[5];
+    }
     const real Fn = dot(F, n);
     const real FT[3] = {F[0] - Fn * n[0], F[1] - Fn * n[1], F[2] - Fn * n[2]};
     real v[3], sp = (real)0, FTn = (real)0;
@@ -157,107 +309,16 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? (STORED ? 6 
         sp = rp.v0 + FTn;
         for (int k = 0; k < 3; ++k) v[k] = sp * p[k];
     }
-    const real vn2 = dot(v, v), mn2 = dot(m, m);
-    const real ivn = vn2 > (real)0 ? d_rsqrt(vn2) : (real)0;
-    const real imn = mn2 > (real)0 ? d_rsqrt(mn2) : (real)0;
-    real pxv[3], pxm[3];
-    cross(p, v, pxv);
-    cross(p, m, pxm);
-    const real A1 = dot(pxv, n), B1 = dot(pxm, n);
-    const real omega = A1 * ivn * rp.inv_tau + rp.align * B1 * imn;
-    real xi, u01 = (real)0.5;
-    if (a.noise) {
-        xi = a.noise[gid];
-    } else {
-        const unsigned bits = tdsr::noise_bits24(a.seed, a.step, local, (unsigned)rep);
-        u01 = (real)bits * (real)(1.0 / 16777216.0);
-        xi = rp.eta * (u01 - (real)0.5);
-    }
-    const real delta = rp.dt * omega + xi;
-    real sd, cd;
-    d_sincos(delta, &sd, &cd);
-    real np[3];
-    cross(n, p, np);
-    const real p2[3] = {cd * p[0] + sd * np[0], cd * p[1] + sd * np[1], cd * p[2] + sd * np[2]};
-    const real w0 = Jp[0] * p2[0] + Jp[1] * p2[1] + Jp[2] * p2[2];
-    const real w1 = Jp[3] * p2[0] + Jp[4] * p2[1] + Jp[5] * p2[2];
-    const real vu = Jp[0] * v[0] + Jp[1] * v[1] + Jp[2] * v[2];
-    const real vv = Jp[3] * v[0] + Jp[4] * v[1] + Jp[5] * v[2];
-    const real u2 = U.x + rp.dt * vu, v2 = U.y + rp.dt * vv;
-    real ex = u2, ey = v2, tvu = vu, tvv = vv, tw0 = w0, tw1 = w1;
-    int nw = 0;
-    seam_wrap(U.x, U.y, ex, ey, tvu, tvv, tw0, tw1, nw);
-    // linear part of the composed gluing maps: the same wrap applied to the unit vectors
-    real R00 = 1, R10 = 0, R01 = 0, R11 = 1;
-    if (nw > 0) {
-        real ex2 = u2, ey2 = v2;
-        int nw2 = 0;
-        seam_wrap(U.x, U.y, ex2, ey2, R00, R10, R01, R11, nw2);
-    }
-    int mode = 0;
-    const int f2 = locate(a.rec, a.adj, a.G, a.bin_start, a.bin_faces, ex, ey, f, mode);
-    const real* h = a.rec + (size_t)f2 * kRec;
-    real r2[3];
-    face_map(h, ex, ey, r2[0], r2[1], r2[2]);
-
-    // ---- reverse ----
-    real ub3x = a.lam_in[3 * (size_t)gid], ub3y = a.lam_in[3 * (size_t)gid + 1];
-    const real thb2 = a.lam_in[3 * (size_t)gid + 2];
-    real rb2[3] = {0, 0, 0}, vb[3] = {0, 0, 0};
-    if (a.r_target) {
-        const real s = (real)(2.0 * a.w_pos) * (real)rp.inv_n;
-        for (int k = 0; k < 3; ++k) rb2[k] += s * (r2[k] - (real)a.r_target[3 * (size_t)gid + k]);
-    }
-    if (a.phib) {
-        // phi = |S| / N_r with S = sum_i normalize((r2_i - c) x v_i); dL/dS per replica (k_adj_phib)
-        const R4<real> sb = a.phib[rep];
-        const real rc3[3] = {r2[0] - a.cx, r2[1] - a.cy, r2[2] - a.cz};
-        real L[3];
-        cross(rc3, v, L);
-        const real Ln2 = dot(L, L);
-        if (sb.w > (real)0 && Ln2 > (real)0) {
-            const real Sb[3] = {sb.x, sb.y, sb.z};
-            const real iL = d_rsqrt(Ln2);
-            const real ell[3] = {L[0] * iL, L[1] * iL, L[2] * iL};
-            const real se = dot(Sb, ell);
-            const real Lb[3] = {(Sb[0] - se * ell[0]) * iL, (Sb[1] - se * ell[1]) * iL, (Sb[2] - se * ell[2]) * iL};
-            real t1[3], t2[3];
-            cross(v, Lb, t1);    // rc3bar = v x Lbar
-            cross(Lb, rc3, t2);  // vbar  += Lbar x rc
-            for (int k = 0; k < 3; ++k) rb2[k] += t1[k], vb[k] += t2[k];
-        }
-    }
-    // r2 = A' + J' (uv3 - a')
-    const R4<real> h2 = rq(h, 2), h3 = rq(h, 3);
-    ub3x += h2.x * rb2[0] + h2.y * rb2[1] + h2.z * rb2[2];
-    ub3y += h2.w * rb2[0] + h3.x * rb2[1] + h3.y * rb2[2];
-    // uv3 = R uv2 + t
-    const real ub2x = R00 * ub3x + R10 * ub3y, ub2y = R01 * ub3x + R11 * ub3y;
-    // uv2 = uv + dt (Jp v)
-    const real velbx = rp.dt * ub2x, velby = rp.dt * ub2y;
-    for (int k = 0; k < 3; ++k) vb[k] += Jp[k] * velbx + Jp[3 + k] * velby;
-    // theta2 = atan2(w1, w0) + const (the gluing rotations only add constants)
-    const real iw2 = (real)1 / (w0 * w0 + w1 * w1);
-    const real wb0 = -w1 * iw2 * thb2, wb1 = w0 * iw2 * thb2;
-    // w = Jp p2
-    real p2b[3];
-    for (int k = 0; k < 3; ++k) p2b[k] = Jp[k] * wb0 + Jp[3 + k] * wb1;
-    // p2 = cos(delta) p + sin(delta) (n x p)
-    const real deltab = p2b[0] * (cd * np[0] - sd * p[0]) + p2b[1] * (cd * np[1] - sd * p[1]) +
-                        p2b[2] * (cd * np[2] - sd * p[2]);
-    real pb[3], p2bxn[3];
-    cross(p2b, n, p2bxn);
-    for (int k = 0; k < 3; ++k) pb[k] = cd * p2b[k] + sd * p2bxn[k];
-    // delta = dt omega + eta (u - 1/2)
-    const real omegab = rp.dt * deltab;
-    // parameter terms in the working precision (GB300 runs FP64 at a small fraction of the FP32 rate)
-    real gv0 = 0, gmu = 0, gtau = 0, galign = 0, geta = 0;
-    if (!a.noise) geta = deltab * (u01 - (real)0.5);
     real mb[3] = {0, 0, 0};
     real nxp[3];
     cross(n, p, nxp);
+    const real vn2 = dot(v, v);
     if (vn2 > (real)0) {
         // omega_1 = A1 / (|v| tau), A1 = p . (v x n)
+        const real ivn = d_rsqrt(vn2);
+        real pxv[3];
+        cross(p, v, pxv);
+        const real A1 = dot(pxv, n);
         const real A1b = omegab * ivn * rp.inv_tau;
         const real vnb = -A1 * ivn * ivn * rp.inv_tau * omegab;
         gtau += -A1 * ivn * rp.inv_tau * rp.inv_tau * omegab;
@@ -265,8 +326,13 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? (STORED ? 6 
         cross(v, n, vxn);
         for (int k = 0; k < 3; ++k) pb[k] += A1b * vxn[k], vb[k] += A1b * nxp[k] + vnb * v[k] * ivn;
     }
+    const real mn2 = dot(m, m);
     if (mn2 > (real)0) {
         // omega_2 = align B1 / |m|, B1 = p . (m x n)
+        const real imn = d_rsqrt(mn2);
+        real pxm[3];
+        cross(p, m, pxm);
+        const real B1 = dot(pxm, n);
         const real B1b = rp.align * omegab * imn;
         const real mnb = -rp.align * B1 * imn * imn * omegab;
         galign += B1 * imn * omegab;
