@@ -65,7 +65,8 @@ struct AdjArgs {
     R4<real>* aF;        // [N] by slot: (Fbar, ubar_direct.x)
     R4<real>* aM;        // [N] by slot: (mbar, ubar_direct.y)
     R4<real>* aP;        // [N] by slot: (pbar_direct, 0)
-    real* gpar;          // [N][kGPar] by global index, in the working precision
+    real* gpar;          // [kGPar][N] by slot, in the working precision (a replica's slots are the
+                         // same range in every step's sorted order)
     int N;
 };
 
@@ -247,9 +248,7 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? (STORED ? 6 
     // ---- reverse of the polarity and velocity update, on values recomputed from the inputs ----
     const R4<real> PL = reload(a.pol, q);
     const int id = reload(a.ids, q);
-    const int rep = (int)((unsigned)id >> a.local_bits);
-    const RepParams<real>& rp = a.reps[rep];
-    const int gid = rp.off + (int)((unsigned)id & ((1u << a.local_bits) - 1u));
+    const RepParams<real>& rp = a.reps[(unsigned)id >> a.local_bits];
     const real* g = a.rec + (size_t)real_to_face(PL.w) * kRec;
     asm volatile("" : "+l"(g));
     const real p[3] = {PL.x, PL.y, PL.z};
@@ -362,12 +361,16 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? (STORED ? 6 
     a.aF[q] = oF;
     a.aM[q] = oM;
     a.aP[q] = oP;
-    real* gp = a.gpar + (size_t)gid * kGPar;
-    gp[G_V0] += gv0;
-    gp[G_MU] += gmu;
-    gp[G_TAU] += gtau;
-    gp[G_ALIGN] += galign;
-    gp[G_ETA] += geta;
+    // by slot: the slots of a replica are the same range in every step's order, so the sums over
+    // that range are the replica's (coalesced, where an index by particle was a random access:
+    // forward+adjoint 2.99e9 -> 3.40e9 particle-steps/s on the 512-replica bumpy-sphere ensemble)
+    real* gp = a.gpar + q;
+    const size_t N = (size_t)a.N;
+    gp[G_V0 * N] += gv0;
+    gp[G_MU * N] += gmu;
+    gp[G_TAU * N] += gtau;
+    gp[G_ALIGN * N] += galign;
+    gp[G_ETA * N] += geta;
 }
 
 template <typename real>
@@ -465,9 +468,9 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 5 : 3)) k_ad
     a.lam_out[3 * (size_t)gid] = ubx;
     a.lam_out[3 * (size_t)gid + 1] = uby;
     a.lam_out[3 * (size_t)gid + 2] = -sn * cb0 + cs * cb1;
-    real* gp = a.gpar + (size_t)gid * kGPar;
-    gp[G_KREP] += gk;
-    gp[G_KADH] += gkadh;
+    real* gp = a.gpar + q;
+    gp[G_KREP * (size_t)a.N] += gk;
+    gp[G_KADH * (size_t)a.N] += gkadh;
 }
 
 // dL/dS of every stored step and replica, once per adjoint run: phi_t = |S_t| / N_r gives
@@ -490,14 +493,15 @@ __global__ void k_adj_phib(const double* phisum, const double* phibar, const Rep
     out[e] = o;
 }
 
-// Per-replica sums of the per-particle parameter terms, in a fixed order (one block per replica).
+// Per-replica sums of the per-slot parameter terms (replica r: slots off[r] .. off[r] + cnt[r] - 1),
+// in a fixed order (one block per replica).
 template <typename real>
-__global__ void k_adj_reduce(const real* gpar, const int* off, const int* cnt, double* out) {
+__global__ void k_adj_reduce(const real* gpar, long long N, const int* off, const int* cnt, double* out) {
     __shared__ double s[256][kGPar];
     const int r = blockIdx.x;
     double acc[kGPar] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int i = off[r] + threadIdx.x; i < off[r] + cnt[r]; i += 256)
-        for (int k = 0; k < kGPar; ++k) acc[k] += (double)gpar[(size_t)i * kGPar + k];
+        for (int k = 0; k < kGPar; ++k) acc[k] += (double)gpar[(size_t)k * N + i];
     for (int k = 0; k < kGPar; ++k) s[threadIdx.x][k] = acc[k];
     __syncthreads();
     for (int w = 128; w > 0; w >>= 1) {

@@ -1281,7 +1281,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
             cur ^= 1;
         }
     }
-    tdsk::k_adj_reduce<real><<<(int)R, 256, 0, s->stream>>>(gpar, d_off, d_cnt, d_gp);
+    tdsk::k_adj_reduce<real><<<(int)R, 256, 0, s->stream>>>(gpar, (long long)N, d_off, d_cnt, d_gp);
     CK(cudaGetLastError());
     snapshot_copy<real>(s, fin, false);  // the handle ends where the forward ended
     std::vector<real> lh(3 * N);
