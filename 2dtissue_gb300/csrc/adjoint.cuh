@@ -60,8 +60,8 @@ struct AdjArgs {
     const double* r_target;  // [3N] by global index, last step only (null otherwise)
     double w_pos;
     // adjoint state
-    const real* lam_in;  // [3N] adjoint of (u, v, theta) after step t
-    real* lam_out;       // [3N] adjoint before step t
+    const real* lam_in;  // [N] x 4 by global index: adjoint of (u, v, theta) after step t, padded to
+    real* lam_out;       //   16 bytes (one vector access); the same before step t
     R4<real>* aF;        // [N] by slot: (Fbar, ubar_direct.x)
     R4<real>* aM;        // [N] by slot: (mbar, ubar_direct.y)
     R4<real>* aP;        // [N] by slot: (pbar_direct, 0)
@@ -210,8 +210,9 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? (STORED ? 6 
         face_map(h, ex, ey, r2[0], r2[1], r2[2]);
 
         // ---- reverse of the new position's terms ----
-        real ub3x = a.lam_in[3 * (size_t)gid], ub3y = a.lam_in[3 * (size_t)gid + 1];
-        thb2 = a.lam_in[3 * (size_t)gid + 2];
+        const R4<real> lin = reinterpret_cast<const R4<real>*>(a.lam_in)[gid];
+        real ub3x = lin.x, ub3y = lin.y;
+        thb2 = lin.z;
         real rb2[3] = {0, 0, 0};
         if (a.r_target) {
             const real s = (real)(2.0 * a.w_pos) * (real)rp.inv_n;
@@ -465,9 +466,9 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 5 : 3)) k_ad
     const real qb[3] = {(pbt[0] - pq * pp[0]) * iq, (pbt[1] - pq * pp[1]) * iq, (pbt[2] - pq * pp[2]) * iq};
     const real cb0 = Ju[0] * qb[0] + Ju[1] * qb[1] + Ju[2] * qb[2];
     const real cb1 = Jv[0] * qb[0] + Jv[1] * qb[1] + Jv[2] * qb[2];
-    a.lam_out[3 * (size_t)gid] = ubx;
-    a.lam_out[3 * (size_t)gid + 1] = uby;
-    a.lam_out[3 * (size_t)gid + 2] = -sn * cb0 + cs * cb1;
+    R4<real> lo;
+    lo.x = ubx, lo.y = uby, lo.z = -sn * cb0 + cs * cb1, lo.w = (real)0;
+    reinterpret_cast<R4<real>*>(a.lam_out)[gid] = lo;
     real* gp = a.gpar + q;
     gp[G_KREP * (size_t)a.N] += gk;
     gp[G_KADH * (size_t)a.N] += gkadh;

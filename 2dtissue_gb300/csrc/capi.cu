@@ -1079,7 +1079,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     const bool keep_sums = s->lanes == 1;
     const size_t b_store = b_state + (M + 1) * sizeof(int) + (keep_sums ? N * (sizeof(R4<real>) + sizeof(R2<real>)) : 0);
     const size_t b_snap = b_state + M * sizeof(int) + 2 * (size_t)s->n_tiles * sizeof(int) + 64;
-    const size_t b_fixed = 2 * 3 * N * sizeof(real) + 3 * N * sizeof(R4<real>) + N * tdsk::kGPar * sizeof(real) +
+    const size_t b_fixed = 2 * 4 * N * sizeof(real) + 3 * N * sizeof(R4<real>) + N * tdsk::kGPar * sizeof(real) +
                            (size_t)T * R * (7 * sizeof(double) + sizeof(R4<real>)) + 3 * N * sizeof(double) + b_snap;
     // checkpoint stride: the largest that fits (one stored segment + the checkpoints)
     int K = sp->checkpoint_stride;
@@ -1123,7 +1123,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
                 ok = ok && x.sum_f && x.sum_m;
             }
         }
-        lam[0] = A.get<real>(3 * N), lam[1] = A.get<real>(3 * N);
+        lam[0] = A.get<real>(4 * N), lam[1] = A.get<real>(4 * N);
         aF = A.get<R4<real>>(N), aM = A.get<R4<real>>(N), aP = A.get<R4<real>>(N);
         gpar = A.get<real>(N * tdsk::kGPar);
         phisum = A.get<double>((size_t)T * R * 6);
@@ -1231,7 +1231,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
 
     // ---- reverse sweep ----
     Range rev("adjoint reverse");
-    CK(cudaMemsetAsync(lam[0], 0, 3 * N * sizeof(real), s->stream));
+    CK(cudaMemsetAsync(lam[0], 0, 4 * N * sizeof(real), s->stream));
     CK(cudaMemsetAsync(gpar, 0, N * tdsk::kGPar * sizeof(real), s->stream));
     if (phi_term)
         tdsk::k_adj_phib<real><<<(unsigned)(((long long)T * R + 255) / 256), 256, 0, s->stream>>>(
@@ -1284,9 +1284,9 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     tdsk::k_adj_reduce<real><<<(int)R, 256, 0, s->stream>>>(gpar, (long long)N, d_off, d_cnt, d_gp);
     CK(cudaGetLastError());
     snapshot_copy<real>(s, fin, false);  // the handle ends where the forward ended
-    std::vector<real> lh(3 * N);
+    std::vector<real> lh(4 * N);
     std::vector<double> gh(R * tdsk::kGPar);
-    CK(cudaMemcpyAsync(lh.data(), lam[cur], 3 * N * sizeof(real), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(lh.data(), lam[cur], 4 * N * sizeof(real), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaMemcpyAsync(gh.data(), d_gp, gh.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     if ((rc = sync_all(s))) return rc;
     res->loss = pre_loss + loss;
@@ -1294,8 +1294,8 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     if (res->d_params)
         for (size_t i = 0; i < gh.size(); ++i) res->d_params[i] = gh[i];
     for (size_t i = 0; i < N; ++i) {
-        if (res->d_uv0) res->d_uv0[2 * i] = (double)lh[3 * i], res->d_uv0[2 * i + 1] = (double)lh[3 * i + 1];
-        if (res->d_theta0) res->d_theta0[i] = (double)lh[3 * i + 2];
+        if (res->d_uv0) res->d_uv0[2 * i] = (double)lh[4 * i], res->d_uv0[2 * i + 1] = (double)lh[4 * i + 1];
+        if (res->d_theta0) res->d_theta0[i] = (double)lh[4 * i + 2];
     }
     return TDS_OK;
 }
