@@ -51,17 +51,24 @@ struct AdjArgs {
     const RepParams<real>* reps;
     int local_bits;
     real cx, cy, cz;
-    long long step;  // noise counter of step t
+    // Step t of the run (0 .. T - 1) is *t0 + j: t0, the first step of the current segment, is
+    // read on the device, so that a segment's reverse launches (j = K - 1 .. 0) are the same for
+    // every segment and are captured once as a CUDA graph.
+    const int* t0;
+    int j;
+    int T;
+    int R;
+    long long step0;  // noise counter of step 0 of the run
     unsigned long long seed;
     const real* noise;  // injected noise of step t by global index, or null
-    // loss terms of step t
-    const R4<real>* phib;    // [R] the order-parameter adjoint of step t per replica: (dL/dS, S != 0),
+    // loss terms
+    const R4<real>* phib;    // [T][R] the order-parameter adjoint per step and replica: (dL/dS, S != 0),
                              // S the step's sum of normalize((r' - c) x v) (null: no order-parameter term)
-    const double* r_target;  // [3N] by global index, last step only (null otherwise)
+    const double* r_target;  // [3N] by global index, the last step's term (null: none)
     double w_pos;
-    // adjoint state
-    const real* lam_in;  // [N] x 4 by global index: adjoint of (u, v, theta) after step t, padded to
-    real* lam_out;       //   16 bytes (one vector access); the same before step t
+    // adjoint state: [N] x 4 by global index, (u, v, theta) padded to 16 bytes (one vector access);
+    // the adjoint after step t is lam[(T - 1 - t) & 1], the one before it the other
+    real* lam[2];
     R4<real>* aF;        // [N] by slot: (Fbar, ubar_direct.x)
     R4<real>* aM;        // [N] by slot: (mbar, ubar_direct.y)
     R4<real>* aP;        // [N] by slot: (pbar_direct, 0)
@@ -123,6 +130,7 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? (STORED ? 6 
     k_adj_a(const AdjArgs<real> a) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= a.N) return;
+    const int t = *a.t0 + a.j;
     real acc[6] = {0, 0, 0, 0, 0, 0};
     real cd, sd, u01 = (real)0.5, ub2x, ub2y, thb2, vb[3] = {0, 0, 0};
     {
@@ -179,7 +187,7 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? (STORED ? 6 
         if (a.noise) {
             xi = a.noise[gid];
         } else {
-            const unsigned bits = tdsr::noise_bits24(a.seed, a.step, local, (unsigned)rep);
+            const unsigned bits = tdsr::noise_bits24(a.seed, a.step0 + t, local, (unsigned)rep);
             u01 = (real)bits * (real)(1.0 / 16777216.0);
             xi = rp.eta * (u01 - (real)0.5);
         }
@@ -210,17 +218,17 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? (STORED ? 6 
         face_map(h, ex, ey, r2[0], r2[1], r2[2]);
 
         // ---- reverse of the new position's terms ----
-        const R4<real> lin = reinterpret_cast<const R4<real>*>(a.lam_in)[gid];
+        const R4<real> lin = reinterpret_cast<const R4<real>*>(a.lam[(a.T - 1 - t) & 1])[gid];
         real ub3x = lin.x, ub3y = lin.y;
         thb2 = lin.z;
         real rb2[3] = {0, 0, 0};
-        if (a.r_target) {
+        if (a.r_target && t == a.T - 1) {
             const real s = (real)(2.0 * a.w_pos) * (real)rp.inv_n;
             for (int k = 0; k < 3; ++k) rb2[k] += s * (r2[k] - (real)a.r_target[3 * (size_t)gid + k]);
         }
         if (a.phib) {
             // phi = |S| / N_r with S = sum_i normalize((r2_i - c) x v_i); dL/dS per replica (k_adj_phib)
-            const R4<real> sb = a.phib[rep];
+            const R4<real> sb = a.phib[(size_t)t * a.R + rep];
             const real rc3[3] = {r2[0] - a.cx, r2[1] - a.cy, r2[2] - a.cz};
             real L[3];
             cross(rc3, v, L);
@@ -468,13 +476,16 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 5 : 3)) k_ad
     const real cb1 = Jv[0] * qb[0] + Jv[1] * qb[1] + Jv[2] * qb[2];
     R4<real> lo;
     lo.x = ubx, lo.y = uby, lo.z = -sn * cb0 + cs * cb1, lo.w = (real)0;
-    reinterpret_cast<R4<real>*>(a.lam_out)[gid] = lo;
+    reinterpret_cast<R4<real>*>(a.lam[(a.T - *a.t0 - a.j) & 1])[gid] = lo;
     real* gp = a.gpar + q;
     gp[G_KREP * (size_t)a.N] += gk;
     gp[G_KADH * (size_t)a.N] += gkadh;
 }
 
 // dL/dS of every stored step and replica, once per adjoint run: phi_t = |S_t| / N_r gives
+// The first step of the segment whose reverse launches follow (read by k_adj_a / k_adj_b).
+__global__ void k_adj_segment(int* t0, int v) { *t0 = v; }
+
 // dL/dS = phibar_t / (N_r |S_t|) S_t (the FP64 square root and division once per replica and step,
 // not once per particle); w = 1 when S_t != 0.
 template <typename real>

@@ -1108,7 +1108,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     real* gpar = nullptr;
     R4<real>* dSb = nullptr;  // dL/dS per stored step and replica (k_adj_phib)
     double *phisum = nullptr, *phibar = nullptr, *rtgt = nullptr, *d_gp = nullptr;
-    int *d_off = nullptr, *d_cnt = nullptr;
+    int *d_off = nullptr, *d_cnt = nullptr, *d_t0 = nullptr;
     // all work buffers come from one block: measured first, then carved
     auto carve = [&](Carve& A) -> bool {
         bool ok = true;
@@ -1130,9 +1130,10 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
         phibar = A.get<double>((size_t)T * R);
         dSb = A.get<R4<real>>((size_t)T * R);
         rtgt = sp->r3d_target ? A.get<double>(3 * N) : nullptr;
-        d_off = A.get<int>(R), d_cnt = A.get<int>(R);
+        d_off = A.get<int>(R), d_cnt = A.get<int>(R), d_t0 = A.get<int>(1);
         d_gp = A.get<double>(R * tdsk::kGPar);
-        return ok && lam[0] && lam[1] && aF && aM && aP && gpar && phisum && phibar && dSb && d_off && d_cnt && d_gp &&
+        return ok && lam[0] && lam[1] && aF && aM && aP && gpar && phisum && phibar && dSb && d_off && d_cnt && d_t0 &&
+               d_gp &&
                (!sp->r3d_target || rtgt);
     };
     {
@@ -1236,7 +1237,6 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     if (phi_term)
         tdsk::k_adj_phib<real><<<(unsigned)(((long long)T * R + 255) / 256), 256, 0, s->stream>>>(
             phisum, phibar, (const RepParams<real>*)s->reps, (int)R, (long long)T * R, dSb);
-    int cur = 0;
     tdsk::AdjArgs<real> a;
     std::memset(&a, 0, sizeof a);
     a.desc = s->desc;
@@ -1253,6 +1253,39 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     a.aF = aF, a.aM = aM, a.aP = aP;
     a.gpar = gpar;
     a.N = s->N;
+    a.t0 = d_t0;
+    a.T = T;
+    a.R = (int)R;
+    a.step0 = t_base;
+    a.phib = phi_term ? dSb : nullptr;
+    a.r_target = (rtgt && sp->w_pos > 0) ? rtgt : nullptr;
+    a.lam[0] = lam[0], a.lam[1] = lam[1];
+    const unsigned nbA = (unsigned)((s->N + tdsk::kAdjThreads - 1) / tdsk::kAdjThreads);
+    // the reverse launches of steps t0 + n - 1 .. t0 of a segment (store slots n - 1 .. 0); t0 is
+    // read on the device, so a full segment's launches are the same for every segment
+    auto reverse_launches = [&](int n) {
+        for (int j = n - 1; j >= 0; --j) {
+            const StepStore& x = store[j];
+            a.pos = (const R4<real>*)x.pos, a.pol = (const R4<real>*)x.pol, a.uv = (const R2<real>*)x.uv;
+            a.ids = x.ids, a.key = x.key, a.start = x.start;
+            a.sum_f = (const R4<real>*)x.sum_f, a.sum_m = (const R2<real>*)x.sum_m;
+            a.j = j;
+            if (a.sum_f)
+                tdsk::k_adj_a<real, true><<<nbA, tdsk::kAdjThreads, 0, s->stream>>>(a);
+            else
+                tdsk::k_adj_a<real, false><<<nbA, tdsk::kAdjThreads, 0, s->stream>>>(a);
+            tdsk::k_adj_b<real><<<nbA, tdsk::kAdjThreads, 0, s->stream>>>(a);
+        }
+    };
+    // A full segment's reverse launches as one CUDA graph (captured once per call): on a small
+    // system the reverse step is launch-bound
+    cudaGraphExec_t rev_graph = nullptr;
+    struct GraphGuard {
+        cudaGraphExec_t* g;
+        ~GraphGuard() {
+            if (*g) cudaGraphExecDestroy(*g);
+        }
+    } rev_guard{&rev_graph};
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int t0 = seg * K, t1 = std::min(T, t0 + K);
         if (seg != nseg - 1) {  // recompute the segment from its checkpoint, storing each step
@@ -1261,24 +1294,25 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
             if ((rc = run_segment(t0, t1, true))) return rc;
             flush_finalize<real>(s);  // the next restore must not finalize this segment's last step
         }
-        for (int t = t1 - 1; t >= t0; --t) {
-            const StepStore& x = store[t - t0];
-            a.pos = (const R4<real>*)x.pos, a.pol = (const R4<real>*)x.pol, a.uv = (const R2<real>*)x.uv;
-            a.ids = x.ids, a.key = x.key, a.start = x.start;
-            a.sum_f = (const R4<real>*)x.sum_f, a.sum_m = (const R2<real>*)x.sum_m;
-            a.step = t_base + t;
-            a.phib = phi_term ? dSb + (size_t)t * R : nullptr;
-            a.r_target = (t == T - 1 && rtgt && sp->w_pos > 0) ? rtgt : nullptr;
-            a.lam_in = lam[cur];
-            a.lam_out = lam[cur ^ 1];
-            if (a.sum_f)
-                tdsk::k_adj_a<real, true><<<(s->N + tdsk::kAdjThreads - 1) / tdsk::kAdjThreads, tdsk::kAdjThreads, 0,
-                                            s->stream>>>(a);
-            else
-                tdsk::k_adj_a<real, false><<<(s->N + tdsk::kAdjThreads - 1) / tdsk::kAdjThreads, tdsk::kAdjThreads, 0,
-                                             s->stream>>>(a);
-            tdsk::k_adj_b<real><<<(s->N + tdsk::kAdjThreads - 1) / tdsk::kAdjThreads, tdsk::kAdjThreads, 0, s->stream>>>(a);
-            cur ^= 1;
+        tdsk::k_adj_segment<<<1, 1, 0, s->stream>>>(d_t0, t0);
+        if (t1 - t0 == K && K > 1 && !s->timing) {
+            if (!rev_graph) {
+                cudaGraph_t graph = nullptr;
+                CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+                reverse_launches(K);
+                const cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+                if (e != cudaSuccess)
+                    return fail(s, TDS_ERR_CUDA, std::string("adjoint reverse capture: ") + cudaGetErrorString(e));
+                const cudaError_t e2 = cudaGraphInstantiate(&rev_graph, graph, 0);
+                cudaGraphDestroy(graph);
+                if (e2 != cudaSuccess) {
+                    rev_graph = nullptr;
+                    return fail(s, TDS_ERR_CUDA, std::string("adjoint reverse graph: ") + cudaGetErrorString(e2));
+                }
+            }
+            CK(cudaGraphLaunch(rev_graph, s->stream));
+        } else {
+            reverse_launches(t1 - t0);
         }
     }
     tdsk::k_adj_reduce<real><<<(int)R, 256, 0, s->stream>>>(gpar, (long long)N, d_off, d_cnt, d_gp);
@@ -1286,7 +1320,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     snapshot_copy<real>(s, fin, false);  // the handle ends where the forward ended
     std::vector<real> lh(4 * N);
     std::vector<double> gh(R * tdsk::kGPar);
-    CK(cudaMemcpyAsync(lh.data(), lam[cur], 4 * N * sizeof(real), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(lh.data(), lam[T & 1], 4 * N * sizeof(real), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaMemcpyAsync(gh.data(), d_gp, gh.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     if ((rc = sync_all(s))) return rc;
     res->loss = pre_loss + loss;
