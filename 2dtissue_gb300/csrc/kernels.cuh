@@ -498,7 +498,12 @@ __device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<re
 // the test and the term (pair_add recomputes the separation) leaves 4 bytes of spills per thread
 // at 40 registers instead of 12: the step kernel 123.0 -> 118.7 us at 1M particles.
 // NBR (a test hook's instantiation): each neighbour's sorted slot is also written to list[0..cap).
-template <typename real, int BLOCK, bool NBR = false>
+// SPEC: both candidates' polarities are loaded with their positions, before the distance tests (one
+// dependent load level per iteration instead of two, at the cost of loading non-neighbours'
+// polarities): the single-system step kernel at 1M particles 109.4 -> 107.2 us, at 10,000
+// particles 21.5 -> 20.6 us per step; on the 6.75M-particle ensemble, whose state does not stay
+// in L2, 571 -> 576 us, so the ensemble kernel keeps the loads behind the tests.
+template <typename real, int BLOCK, bool NBR = false, bool SPEC = false>
 __device__ __forceinline__ void pair_sums_s(const PairC<real>& pc, const R4<real>& P, const R4<real>* __restrict__ pos,
                                           const R4<real>* __restrict__ pol, const int2* srun, int total, int self,
                                           real (&acc)[6], int& cnt, int* list = nullptr, int cap = 0) {
@@ -528,11 +533,14 @@ __device__ __forceinline__ void pair_sums_s(const PairC<real>& pc, const R4<real
         }
         const R4<real> Qa = pos[ta];
         const R4<real> Qb = pos[tb >= 0 ? tb : ta];
+        R4<real> La, Lb;
+        if (SPEC) La = pol[ta], Lb = pol[tb >= 0 ? tb : ta];
         const bool na = pair_d2(P, Qa) < pc.r_max2 && ta != self;
         const bool nb = tb >= 0 && pair_d2(P, Qb) < pc.r_max2 && tb != self;
-        R4<real> La, Lb;
-        if (na) La = pol[ta];
-        if (nb) Lb = pol[tb];
+        if (!SPEC) {
+            if (na) La = pol[ta];
+            if (nb) Lb = pol[tb];
+        }
         if (na) {
             if (NBR && cnt < cap) list[cnt] = ta;
             pair_add(pc, P, Qa, La, acc, cnt);
@@ -648,7 +656,8 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
                         : nullptr;
         if (LPP == 1) {
             if (a.single)
-                pair_sums_s<real, BLOCK, NBR>(a.pc0, P, a.pos, a.pol, srun, total, q, acc, cnt, list, a.nbr_cap);
+                pair_sums_s<real, BLOCK, NBR, SINGLE>(a.pc0, P, a.pos, a.pol, srun, total, q, acc, cnt, list,
+                                                      a.nbr_cap);
             else
                 pair_sums_s<real, BLOCK, NBR>(pair_constants(rp), P, a.pos, a.pol, srun, total, q, acc, cnt, list,
                                               a.nbr_cap);
