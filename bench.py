@@ -429,7 +429,9 @@ def ensemble_leg(tg, steps=50, sample=64, autotune=False, replicas=4096):
             "batched_over_one_by_one": batched / one_by_one,
             "batched_over_concurrent_streams": batched / concurrent,
             "roofline": {"bound": "hbm", "achieved": alg / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-                         "frac": alg / (k_ms * 1e-3) / 1e9 / peak, "traffic": None, "peak_source": peak_kind,
+                         "frac": alg / (k_ms * 1e-3) / 1e9 / peak,
+                         "traffic": profiled_traffic("k_step_ensemble_4096_replicas.md", total),
+                         "peak_source": peak_kind,
                          "kernel": "k_step", "kernel_ms": k_ms, "algorithmic_bytes": alg},
             "step_ms_graph_launched": ms / steps, "step_ms_kernels_summed": summed_ms,
             "tuning": sim_tuning, "autotuned": bool(autotune),
