@@ -121,6 +121,8 @@ struct tds_sim {
     // state transfers: uploads and downloads on their own streams, so that the two directions of
     // the host link run at the same time; events order them against the compute stream
     cudaStream_t up = nullptr, down = nullptr;
+    // the adjoint's reverse sweep (created on first use), beside the recompute on the compute stream
+    cudaStream_t rev = nullptr;
     cudaEvent_t ev_in_ready[2] = {nullptr, nullptr}, ev_in_free[2] = {nullptr, nullptr};
     cudaEvent_t ev_out_ready[2] = {nullptr, nullptr}, ev_out_free[2] = {nullptr, nullptr};
     int cur = 0;
@@ -1099,10 +1101,22 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     }
     K = std::min(K, T);
     const int nseg = (T + K - 1) / K;
+    // Two sets of store slots when the memory allows: the reverse sweep of a segment (on the
+    // handle's reverse stream) then runs beside the recompute of the segment before it (on the
+    // compute stream), which writes the other set. On a small system both are latency-bound and
+    // fill a fraction of the GPU, so they overlap almost fully.
+    bool two_sets = false;
+    if (nseg > 1) {
+        size_t fr = 0, tot = 0;
+        CK(cudaMemGetInfo(&fr, &tot));
+        fr += s->adj_ws_bytes;
+        const double budget = fr > b_fixed ? 0.8 * (double)(fr - b_fixed) : 0.0;
+        two_sets = (double)nseg * (double)b_snap + 2.0 * (double)K * (double)b_store <= budget;
+    }
 
     std::vector<Snapshot<real>> snaps(nseg);
     Snapshot<real> fin;
-    std::vector<StepStore> store(K);
+    std::vector<StepStore> store((size_t)(two_sets ? 2 : 1) * K);
     real* lam[2] = {nullptr, nullptr};
     R4<real>*aF = nullptr, *aM = nullptr, *aP = nullptr;
     real* gpar = nullptr;
@@ -1171,10 +1185,11 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     // and once with it (the forward's last segment and every recomputed segment). On a small
     // system the step is launch-bound and the graphs remove the launch gaps.
     SegGraphs<real> sg(s, K, &hk, store.data());
-    auto run_segment = [&](int t0, int t1, bool stored) -> int {
-        if (t1 - t0 == K && !s->timing) return sg.launch(stored);
+    SegGraphs<real> sg1(s, K, &hk, store.data() + (two_sets ? K : 0));
+    auto run_segment = [&](int t0, int t1, bool stored, int set) -> int {
+        if (t1 - t0 == K && !s->timing) return (set ? sg1 : sg).launch(stored);
         for (int t = t0; t < t1; ++t) {
-            hk.store = stored ? &store[t - t0] : nullptr;
+            hk.store = stored ? &store[(size_t)set * K + (t - t0)] : nullptr;
             launch_one_step<real>(s, nullptr, &hk);
         }
         return TDS_OK;
@@ -1183,7 +1198,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
         Range fwd("adjoint forward");
         for (int seg = 0; seg < nseg; ++seg) {
             snapshot_copy<real>(s, snaps[seg], true);
-            if ((rc = run_segment(seg * K, std::min(T, seg * K + K), seg == nseg - 1))) return rc;
+            if ((rc = run_segment(seg * K, std::min(T, seg * K + K), seg == nseg - 1, 0))) return rc;
         }
         flush_finalize<real>(s, &hk);
     }
@@ -1261,60 +1276,96 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     a.r_target = (rtgt && sp->w_pos > 0) ? rtgt : nullptr;
     a.lam[0] = lam[0], a.lam[1] = lam[1];
     const unsigned nbA = (unsigned)((s->N + tdsk::kAdjThreads - 1) / tdsk::kAdjThreads);
-    // the reverse launches of steps t0 + n - 1 .. t0 of a segment (store slots n - 1 .. 0); t0 is
-    // read on the device, so a full segment's launches are the same for every segment
-    auto reverse_launches = [&](int n) {
+    if (!s->rev && cudaStreamCreateWithFlags(&s->rev, cudaStreamNonBlocking) != cudaSuccess) {
+        s->rev = nullptr;
+        return fail(s, TDS_ERR_CUDA, "adjoint: reverse stream");
+    }
+    cudaStream_t rs = s->rev;
+    // events: [0] the reverse may start / the reverse is done, [1..2] store set recomputed,
+    // [3..4] store set read by its reverse sweep
+    struct Events {
+        cudaEvent_t e[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+        ~Events() {
+            for (cudaEvent_t x : e)
+                if (x) cudaEventDestroy(x);
+        }
+    } ev;
+    for (cudaEvent_t& x : ev.e) CK(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+    cudaEvent_t* ev_rec = ev.e + 1;
+    cudaEvent_t* ev_read = ev.e + 3;
+    CK(cudaEventRecord(ev.e[0], s->stream));
+    CK(cudaStreamWaitEvent(rs, ev.e[0], 0));
+    // the reverse launches of steps t0 + n - 1 .. t0 of a segment (slots n - 1 .. 0 of a store set);
+    // t0 is read on the device, so a full segment's launches are the same for every segment
+    auto reverse_launches = [&](int n, const StepStore* base) {
         for (int j = n - 1; j >= 0; --j) {
-            const StepStore& x = store[j];
+            const StepStore& x = base[j];
             a.pos = (const R4<real>*)x.pos, a.pol = (const R4<real>*)x.pol, a.uv = (const R2<real>*)x.uv;
             a.ids = x.ids, a.key = x.key, a.start = x.start;
             a.sum_f = (const R4<real>*)x.sum_f, a.sum_m = (const R2<real>*)x.sum_m;
             a.j = j;
             if (a.sum_f)
-                tdsk::k_adj_a<real, true><<<nbA, tdsk::kAdjThreads, 0, s->stream>>>(a);
+                tdsk::k_adj_a<real, true><<<nbA, tdsk::kAdjThreads, 0, rs>>>(a);
             else
-                tdsk::k_adj_a<real, false><<<nbA, tdsk::kAdjThreads, 0, s->stream>>>(a);
-            tdsk::k_adj_b<real><<<nbA, tdsk::kAdjThreads, 0, s->stream>>>(a);
+                tdsk::k_adj_a<real, false><<<nbA, tdsk::kAdjThreads, 0, rs>>>(a);
+            tdsk::k_adj_b<real><<<nbA, tdsk::kAdjThreads, 0, rs>>>(a);
         }
     };
-    // A full segment's reverse launches as one CUDA graph (captured once per call): on a small
-    // system the reverse step is launch-bound
-    cudaGraphExec_t rev_graph = nullptr;
-    struct GraphGuard {
-        cudaGraphExec_t* g;
-        ~GraphGuard() {
-            if (*g) cudaGraphExecDestroy(*g);
+    // A full segment's reverse launches as one CUDA graph per store set (captured once per call):
+    // on a small system the reverse step is launch-bound
+    struct Graphs {
+        cudaGraphExec_t g[2] = {nullptr, nullptr};
+        ~Graphs() {
+            for (cudaGraphExec_t x : g)
+                if (x) cudaGraphExecDestroy(x);
         }
-    } rev_guard{&rev_graph};
+    } rgraph;
+    // the recompute of segment g into store set `set` (compute stream), after the reverse sweep that
+    // last read that set
+    auto recompute = [&](int g, int set) -> int {
+        CK(cudaStreamWaitEvent(s->stream, ev_read[set], 0));
+        snapshot_copy<real>(s, snaps[g], false);
+        // (the order-parameter sums of these steps are written again, with the same values)
+        int r = run_segment(g * K, std::min(T, g * K + K), true, set);
+        if (r) return r;
+        flush_finalize<real>(s);  // the next restore must not finalize this segment's last step
+        CK(cudaEventRecord(ev_rec[set], s->stream));
+        return TDS_OK;
+    };
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int t0 = seg * K, t1 = std::min(T, t0 + K);
-        if (seg != nseg - 1) {  // recompute the segment from its checkpoint, storing each step
-            snapshot_copy<real>(s, snaps[seg], false);
-            // (the order-parameter sums of these steps are written again, with the same values)
-            if ((rc = run_segment(t0, t1, true))) return rc;
-            flush_finalize<real>(s);  // the next restore must not finalize this segment's last step
-        }
-        tdsk::k_adj_segment<<<1, 1, 0, s->stream>>>(d_t0, t0);
+        const int set = two_sets ? (nseg - 1 - seg) & 1 : 0;
+        // the last segment's store is the forward's; an earlier one is recomputed from its checkpoint:
+        // with two sets, the segment before this one is recomputed now, beside this one's reverse
+        if (!two_sets && seg != nseg - 1 && (rc = recompute(seg, 0))) return rc;
+        if (two_sets && seg >= 1 && (rc = recompute(seg - 1, set ^ 1))) return rc;
+        if (seg != nseg - 1) CK(cudaStreamWaitEvent(rs, ev_rec[set], 0));
+        const StepStore* base = store.data() + (size_t)set * K;
+        tdsk::k_adj_segment<<<1, 1, 0, rs>>>(d_t0, t0);
         if (t1 - t0 == K && K > 1 && !s->timing) {
-            if (!rev_graph) {
+            cudaGraphExec_t& g = rgraph.g[set];
+            if (!g) {
                 cudaGraph_t graph = nullptr;
-                CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-                reverse_launches(K);
-                const cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+                CK(cudaStreamBeginCapture(rs, cudaStreamCaptureModeThreadLocal));
+                reverse_launches(K, base);
+                const cudaError_t e = cudaStreamEndCapture(rs, &graph);
                 if (e != cudaSuccess)
                     return fail(s, TDS_ERR_CUDA, std::string("adjoint reverse capture: ") + cudaGetErrorString(e));
-                const cudaError_t e2 = cudaGraphInstantiate(&rev_graph, graph, 0);
+                const cudaError_t e2 = cudaGraphInstantiate(&g, graph, 0);
                 cudaGraphDestroy(graph);
                 if (e2 != cudaSuccess) {
-                    rev_graph = nullptr;
+                    g = nullptr;
                     return fail(s, TDS_ERR_CUDA, std::string("adjoint reverse graph: ") + cudaGetErrorString(e2));
                 }
             }
-            CK(cudaGraphLaunch(rev_graph, s->stream));
+            CK(cudaGraphLaunch(g, rs));
         } else {
-            reverse_launches(t1 - t0);
+            reverse_launches(t1 - t0, base);
         }
+        CK(cudaEventRecord(ev_read[set], rs));
     }
+    CK(cudaEventRecord(ev.e[0], rs));
+    CK(cudaStreamWaitEvent(s->stream, ev.e[0], 0));
     tdsk::k_adj_reduce<real><<<(int)R, 256, 0, s->stream>>>(gpar, (long long)N, d_off, d_cnt, d_gp);
     CK(cudaGetLastError());
     snapshot_copy<real>(s, fin, false);  // the handle ends where the forward ended
@@ -1862,6 +1913,7 @@ void tds_destroy(tds_sim* s) {
     if (s->up) cudaStreamSynchronize(s->up);
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->down) cudaStreamSynchronize(s->down);
+    if (s->rev) cudaStreamSynchronize(s->rev);
     collect_times(s);
     for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
     free_graphs(s);
@@ -1876,6 +1928,7 @@ void tds_destroy(tds_sim* s) {
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->up) cudaStreamDestroy(s->up);
     if (s->down) cudaStreamDestroy(s->down);
+    if (s->rev) cudaStreamDestroy(s->rev);
     delete s;
 }
 
