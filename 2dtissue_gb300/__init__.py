@@ -42,7 +42,7 @@ class _Params(C.Structure):
 class _AdjSpec(C.Structure):
     _fields_ = [("n_steps", C.c_int), ("checkpoint_stride", C.c_int), ("r3d_target", C.c_void_p),
                 ("w_pos", C.c_double), ("phi_target", C.c_void_p), ("w_phi", C.c_double), ("window", C.c_int),
-                ("reserved", C.c_int)]
+                ("gather_lanes", C.c_int)]
 
 
 class _AdjResult(C.Structure):
@@ -374,17 +374,18 @@ class Simulation:
         self.params = ps
 
     def adjoint(self, n_steps, r3d_target=None, w_pos=0.0, phi_target=None, w_phi=0.0, checkpoint_stride=0,
-                window=0):
+                window=0, gather_lanes=0):
         """Runs n_steps forward from the current state, then the hand-written reverse sweep.
         Loss = w_pos * sum_r mean_i |r_T - r*|^2 + w_phi * sum_t sum_r (phi_t - phi*_t)^2.
         Returns loss, d_params (R x 7, order GRAD_PARAMS), d_uv0 (N x 2), d_theta0 (N) and the
         checkpoint stride used. window (0 < window < n_steps): truncated gradient over the last
-        `window` steps; d_uv0 / d_theta0 are then with respect to the state at the window's start."""
+        `window` steps; d_uv0 / d_theta0 are then with respect to the state at the window's start.
+        gather_lanes: lanes per particle of the reverse neighbour gather (0 = by system size, 1, 4)."""
         N, R = self.N, self.R
         tgt = None if r3d_target is None else np.ascontiguousarray(r3d_target, np.float64).reshape(N, 3)
         phi = None if phi_target is None else np.ascontiguousarray(phi_target, np.float64).reshape(n_steps, R)
         spec = _AdjSpec(int(n_steps), int(checkpoint_stride), _ptr(tgt), float(w_pos), _ptr(phi), float(w_phi),
-                        int(window), 0)
+                        int(window), int(gather_lanes))
         dp = np.zeros((R, 8))
         duv = np.zeros((N, 2))
         dth = np.zeros(N)

@@ -382,10 +382,14 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? (STORED ? 6 
     gp[G_ETA * N] += geta;
 }
 
-template <typename real>
+template <typename real, int LPP>
 __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 5 : 3)) k_adj_b(const AdjArgs<real> a) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= a.N) return;
+    const int q0 = (int)((blockIdx.x * blockDim.x + threadIdx.x) / LPP);
+    const int sub = LPP > 1 ? (int)(threadIdx.x % LPP) : 0;
+    if (LPP == 1 && q0 >= a.N) return;
+    // with several lanes per particle, the lanes of a particle past the end stay for the group sums
+    const bool active = q0 < a.N;
+    const int q = active ? q0 : a.N - 1;
     const R4<real> P = a.pos[q];
     const R4<real> PL = a.pol[q];
     const int id = a.ids[q];
@@ -427,9 +431,46 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 5 : 3)) k_ad
                 gkadh += -Fe * (d - rp.twoR) * inv_w;
         }
     };
-    // two candidates per iteration: both distance tests (the forward's neighbour test, rounded the
-    // same way) before either neighbour's terms
-    if (total > 0) {
+    if (LPP > 1) {
+        // lane `sub` takes the candidates sub, sub + LPP, ... of the visiting order; the group's
+        // partial sums are added with a fixed butterfly below
+        const int mine = total > sub ? (total - sub + LPP - 1) / LPP : 0;
+        const int2* sp = run;
+        int t = 0, left = 0;
+        if (total > 0) {
+            const int2 x0 = *sp;
+            t = x0.x, left = x0.y;
+        }
+        int skip = sub;
+        for (int i = 0; i < mine; ++i) {
+            while (skip >= left) {
+                skip -= left;
+                sp += kAdjThreads;
+                const int2 x = *sp;
+                t = x.x, left = x.y;
+            }
+            t += skip, left -= skip;
+            const int tj = t++;
+            --left;
+            skip = LPP - 1;
+            const R4<real> Q = a.pos[tj];
+            if (pair_d2(P, Q) < rp.r_max2 && tj != q) nbr_term(tj, Q);
+        }
+        const unsigned gm = ((1u << LPP) - 1u) << ((threadIdx.x & 31) & ~(unsigned)(LPP - 1));
+#pragma unroll
+        for (int o = 1; o < LPP; o <<= 1) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                rb[k] += __shfl_xor_sync(gm, rb[k], o);
+                msum[k] += __shfl_xor_sync(gm, msum[k], o);
+            }
+            gk += __shfl_xor_sync(gm, gk, o);
+            gkadh += __shfl_xor_sync(gm, gkadh, o);
+        }
+        if (sub != 0 || !active) return;
+    } else if (total > 0) {
+        // two candidates per iteration: both distance tests (the forward's neighbour test, rounded
+        // the same way) before either neighbour's terms
         const int2* sp = run;
         int2 x0 = *sp;
         int t = x0.x, left = x0.y;

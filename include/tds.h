@@ -224,7 +224,11 @@ typedef struct tds_adjoint_spec {
      * explicit-Euler contact step can multiply a separation error by |1 - 2 dt mu k / 2R|) and
      * overflows; the window bounds that growth. */
     int window;
-    int reserved;
+    /* lanes per particle of the reverse step's neighbour gather: 0 = by system size (4 below
+     * 131,072 particles, where one particle's chain of candidate loads sets the time, else 1), or
+     * 1 or 4. The gradients agree to rounding (the lanes' partial sums are added in a fixed order,
+     * so each choice is deterministic). */
+    int gather_lanes;
 } tds_adjoint_spec;
 typedef struct tds_adjoint_result {
     double loss;

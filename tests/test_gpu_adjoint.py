@@ -252,3 +252,44 @@ def test_windowed_adjoint_is_the_adjoint_of_its_window(tg, mesh_l4, precision):
     rc = c.adjoint(T, r3d_target=tgt, w_pos=1.0, phi_target=phit, w_phi=1.0, window=T)
     rd = d.adjoint(T, r3d_target=tgt, w_pos=1.0, phi_target=phit, w_phi=1.0)
     np.testing.assert_array_equal(rc["d_params"], rd["d_params"])
+
+
+def test_gather_lanes_agree(tg, orc, mesh_l4, adj_setup):
+    """The reverse neighbour gather with one and with four lanes per particle (the choice by system
+    size, or the caller's): the same gradients to rounding (FP64), each equal to the dual-number
+    oracle's directional derivative, each deterministic; other widths are refused."""
+    om, cen = adj_setup
+    res = {}
+    for lanes in (1, 4):
+        sim = _start(tg, mesh_l4, 64)
+        s0 = sim.get_state()
+        tgt = s0["r3d"] + 0.01
+        phit = np.full(T, 0.3)
+        res[lanes] = [sim.adjoint(T, r3d_target=tgt, w_pos=1.0, phi_target=phit, w_phi=1.0, gather_lanes=lanes)]
+        sim2 = _start(tg, mesh_l4, 64)
+        res[lanes].append(sim2.adjoint(T, r3d_target=tgt, w_pos=1.0, phi_target=phit, w_phi=1.0,
+                                       gather_lanes=lanes))
+    for lanes in (1, 4):
+        for k in ("d_params", "d_uv0", "d_theta0"):
+            np.testing.assert_array_equal(res[lanes][0][k], res[lanes][1][k], err_msg=k)
+    for k in ("d_params", "d_uv0", "d_theta0"):
+        np.testing.assert_allclose(res[1][0][k], res[4][0][k], rtol=1e-9, atol=1e-12 * np.abs(res[1][0][k]).max(),
+                                   err_msg=k)
+    # the default (by size: four lanes at this size) is the four-lane gather
+    sim = _start(tg, mesh_l4, 64)
+    s0 = sim.get_state()
+    r0 = sim.adjoint(T, r3d_target=s0["r3d"] + 0.01, w_pos=1.0, phi_target=np.full(T, 0.3), w_phi=1.0)
+    np.testing.assert_array_equal(r0["d_uv0"], res[4][0]["d_uv0"])
+    # against the oracle's directional derivative along a random parameter direction
+    rng = np.random.default_rng(3)
+    prm = sim.params[0].oracle_dict()
+    direction = rng.normal(size=len(tg.GRAD_PARAMS))
+    dprm = {k: 0.0 for k in prm}
+    for j, name in enumerate(tg.GRAD_PARAMS):
+        dprm[GRAD_TO_ORACLE[name]] = direction[j]
+    _, dl = _oracle_chain(orc, om, cen, prm, s0, 2, dprm, np.zeros((N, 2)), np.zeros(N), s0["r3d"] + 0.01,
+                          np.full(T, 0.3))
+    for lanes in (1, 4):
+        np.testing.assert_allclose(res[lanes][0]["d_params"][0] @ direction, dl, rtol=1e-6)
+    with pytest.raises(tg.TdsError):
+        sim.adjoint(T, r3d_target=s0["r3d"], w_pos=1.0, gather_lanes=2)
