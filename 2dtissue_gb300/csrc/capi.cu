@@ -924,6 +924,7 @@ int sync_all(tds_sim* s) {
     CK(cudaStreamSynchronize(s->up));
     CK(cudaStreamSynchronize(s->stream));
     CK(cudaStreamSynchronize(s->down));
+    if (s->rev) CK(cudaStreamSynchronize(s->rev));  // an adjoint that returned early leaves nothing in flight
     if (int rc = take_refused_load(s, "set_state_async")) return rc;
     int st = 0;
     CK(cudaMemcpy(&st, s->status, sizeof(int), cudaMemcpyDeviceToHost));
