@@ -40,7 +40,7 @@ struct AdjArgs {
     const int* ids;
     const int* key;
     const int* start;
-    const R4<real>* sum_f;  // step t's pair sums by slot (F, m.x), (m.y, m.z), or null (recomputed)
+    const R4<real>* sum_f;  // step t's pair sums by slot, as its step kernel stored them: (F, m.x), (m.y, m.z)
     const R2<real>* sum_m;
     const uint4* desc;
     const real* rec;
@@ -116,22 +116,19 @@ __device__ __forceinline__ real dot(const real a[3], const real b[3]) {
     return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
 }
 
-// STORED: the forward stored this step's pair sums (a.sum_f, a.sum_m), so the kernel has no pair
-// loop and fewer registers; otherwise the sums are recomputed with the step kernel's own loop.
-// Two phases, so that few values are live at any point: the forward recompute runs through the
+// The pair sums are the ones the forward's step kernel stored for this step (a.sum_f, a.sum_m:
+// its own values, whatever its lanes per particle), so the kernel has no pair loop. Two phases, so that few values are live at any point: the forward recompute runs through the
 // step's discrete decisions (seam wraps, the new face) and the new position, whose adjoint terms
 // are taken at once; the reverse of the polarity and velocity update then recomputes what it
 // needs from the step's inputs, read again (L1/L2 hits), rather than keeping the forward's
 // intermediates live (or spilled) across the wrap and the location: FP32 spills 180/356 -> 60/52
-// bytes per thread at 6 blocks per SM (0/0 with the pair loop at 4), forward+adjoint +1.5% on the
-// 512-replica bumpy-sphere ensemble, the results unchanged.
-template <typename real, bool STORED>
-__global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? (STORED ? 6 : 4) : 2))
-    k_adj_a(const AdjArgs<real> a) {
+// bytes per thread at 6 blocks per SM, forward+adjoint +1.5% on the 512-replica bumpy-sphere
+// ensemble, the results unchanged.
+template <typename real>
+__global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? 6 : 2)) k_adj_a(const AdjArgs<real> a) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= a.N) return;
     const int t = *a.t0 + a.j;
-    real acc[6] = {0, 0, 0, 0, 0, 0};
     real cd, sd, u01 = (real)0.5, ub2x, ub2y, thb2, vb[3] = {0, 0, 0};
     {
         const R4<real> PL = a.pol[q];
@@ -144,24 +141,12 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? (STORED ? 6 
         const int f = real_to_face(PL.w);
         const real* g = a.rec + (size_t)f * kRec;
 
-        // ---- forward recompute (the arithmetic of k_step) ----
-        if (STORED) {
-            // the pair sums the forward step stored (the step kernel's own values)
-            const R4<real> sf = a.sum_f[q];
-            const R2<real> sm = a.sum_m[q];
-            acc[0] = sf.x, acc[1] = sf.y, acc[2] = sf.z, acc[3] = sf.w, acc[4] = sm.x, acc[5] = sm.y;
-        } else {
-            __shared__ int2 s_run[9 * kAdjThreads];
-            int2* run = s_run + threadIdx.x;
-            const R4<real> P = a.pos[q];
-            const int total = candidate_runs(rp, a.desc, a.start, a.key[q], run);
-            int cnt = 0;
-            // the step kernel's own pair loop (same visiting order and arithmetic: the same sums, bit for bit)
-            pair_sums_s<real, kAdjThreads>(pair_constants(rp), P, a.pos, a.pol, run, total, q, acc, cnt);
-        }
+        // ---- forward recompute (the arithmetic of k_step), from the stored pair sums ----
+        const R4<real> sf = a.sum_f[q];
+        const R2<real> sm = a.sum_m[q];
         const real p[3] = {PL.x, PL.y, PL.z};
-        const real F[3] = {acc[0], acc[1], acc[2]};
-        const real m[3] = {acc[3], acc[4], acc[5]};
+        const real F[3] = {sf.x, sf.y, sf.z};
+        const real m[3] = {sf.w, sm.x, sm.y};
         real n[3], Jp[6];
         face_frame(g, n, Jp);
         const real Fn = dot(F, n);
@@ -297,15 +282,10 @@ __global__ void __launch_bounds__(kAdjThreads, (sizeof(real) == 4 ? (STORED ? 6 
     // parameter terms in the working precision (GB300 runs FP64 at a small fraction of the FP32 rate)
     real gv0 = 0, gmu = 0, gtau = 0, galign = 0, geta = 0;
     if (!a.noise) geta = deltab * (u01 - (real)0.5);
-    // the pair sums again: stored (read again) or kept from the forward recompute
-    real F[3], m[3];
-    if (STORED) {
-        const R4<real> sf = reload(a.sum_f, q);
-        const R2<real> sm = reload(a.sum_m, q);
-        F[0] = sf.x, F[1] = sf.y, F[2] = sf.z, m[0] = sf.w, m[1] = sm.x, m[2] = sm.y;
-    } else {
-        F[0] = acc[0], F[1] = acc[1], F[2] = acc[2], m[0] = acc[3], m[1] = acc[4], m[2] = acc[5];
-    }
+    // the stored pair sums, read again
+    const R4<real> sf = reload(a.sum_f, q);
+    const R2<real> sm = reload(a.sum_m, q);
+    const real F[3] = {sf.x, sf.y, sf.z}, m[3] = {sf.w, sm.x, sm.y};
     const real Fn = dot(F, n);
     const real FT[3] = {F[0] - Fn * n[0], F[1] - Fn * n[1], F[2] - Fn * n[2]};
     real v[3], sp = (real)0, FTn = (real)0;

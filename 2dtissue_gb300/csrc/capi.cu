@@ -574,7 +574,12 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
     {
         KernelTimer kt(s, 3);
         const long long lanes = (long long)s->N * s->lanes;
-        if (a.sum_f && s->R == 1)  // a stored step of the adjoint (one lane per particle): bit-identical
+        // a stored step of the adjoint: the same sums as the plain step of the same tuning, bit for bit
+        if (a.sum_f && s->lanes == 2)
+            tdsk::k_step<real, 128, false, 2, false, true><<<(unsigned)((lanes + 127) / 128), 128, 0, st>>>(a);
+        else if (a.sum_f && s->lanes == 4)
+            tdsk::k_step<real, 128, false, 4, false, true><<<(unsigned)((lanes + 127) / 128), 128, 0, st>>>(a);
+        else if (a.sum_f && s->R == 1)
             tdsk::k_step<real, 128, false, 1, true, true><<<(s->N + 127) / 128, 128, 0, st>>>(a);
         else if (a.sum_f)
             tdsk::k_step<real, 128, false, 1, false, true><<<(s->N + 127) / 128, 128, 0, st>>>(a);
@@ -1081,8 +1086,8 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     const size_t b_state = N * (2 * sizeof(R4<real>) + sizeof(R2<real>) + 2 * sizeof(int));
     // the stored steps keep their pair sums (24 B per particle in FP32) when the step kernel runs one
     // lane per particle (with more lanes its sums round differently from the reverse step's loop)
-    const bool keep_sums = s->lanes == 1;
-    const size_t b_store = b_state + (M + 1) * sizeof(int) + (keep_sums ? N * (sizeof(R4<real>) + sizeof(R2<real>)) : 0);
+    // a stored step keeps its pair sums (24 B per particle in FP32), as the step kernel computed them
+    const size_t b_store = b_state + (M + 1) * sizeof(int) + N * (sizeof(R4<real>) + sizeof(R2<real>));
     const size_t b_snap = b_state + M * sizeof(int) + 2 * (size_t)s->n_tiles * sizeof(int) + 64;
     const size_t b_fixed = 2 * 4 * N * sizeof(real) + 3 * N * sizeof(R4<real>) + N * tdsk::kGPar * sizeof(real) +
                            (size_t)T * R * (7 * sizeof(double) + sizeof(R4<real>)) + 3 * N * sizeof(double) + b_snap;
@@ -1134,11 +1139,8 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
         for (auto& x : store) {
             x.pos = A.get<R4<real>>(N), x.pol = A.get<R4<real>>(N), x.uv = A.get<R2<real>>(N);
             x.ids = A.get<int>(N), x.key = A.get<int>(N), x.start = A.get<int>(M + 1);
-            ok = ok && x.pos && x.pol && x.uv && x.ids && x.key && x.start;
-            if (keep_sums) {
-                x.sum_f = A.get<R4<real>>(N), x.sum_m = A.get<R2<real>>(N);
-                ok = ok && x.sum_f && x.sum_m;
-            }
+            x.sum_f = A.get<R4<real>>(N), x.sum_m = A.get<R2<real>>(N);
+            ok = ok && x.pos && x.pol && x.uv && x.ids && x.key && x.start && x.sum_f && x.sum_m;
         }
         lam[0] = A.get<real>(4 * N), lam[1] = A.get<real>(4 * N);
         aF = A.get<R4<real>>(N), aM = A.get<R4<real>>(N), aP = A.get<R4<real>>(N);
@@ -1312,10 +1314,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
             a.ids = x.ids, a.key = x.key, a.start = x.start;
             a.sum_f = (const R4<real>*)x.sum_f, a.sum_m = (const R2<real>*)x.sum_m;
             a.j = j;
-            if (a.sum_f)
-                tdsk::k_adj_a<real, true><<<nbA, tdsk::kAdjThreads, 0, rs>>>(a);
-            else
-                tdsk::k_adj_a<real, false><<<nbA, tdsk::kAdjThreads, 0, rs>>>(a);
+            tdsk::k_adj_a<real><<<nbA, tdsk::kAdjThreads, 0, rs>>>(a);
             if (glanes == 4)
                 tdsk::k_adj_b<real, 4><<<nbB, tdsk::kAdjThreads, 0, rs>>>(a);
             else

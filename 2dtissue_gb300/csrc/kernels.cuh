@@ -598,8 +598,8 @@ __device__ __forceinline__ void pair_sums_lanes(const PairC<real>& pc, const R4<
 // bank: operands of the arithmetic, no loads) instead of the replica table (2.2% faster at 1M
 // particles, results bit-identical).
 // STORE: a step whose sorted state the adjoint keeps also stores its pair sums (force F and
-// neighbour polarity sum m, by slot), so that the reverse step reads them instead of running the
-// pair loop again.
+// neighbour polarity sum m, by slot; with several lanes per particle the group's sums, by its first
+// lane), so that the reverse step reads the forward's own values instead of running a pair loop.
 template <typename real, int BLOCK, bool NBR = false, int LPP = 1, bool SINGLE = false, bool STORE = false>
 __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLOCK) k_step(const StepArgs<real> a) {
     typedef R4<real> r4;
@@ -672,7 +672,7 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
                 cnt += __shfl_xor_sync(gm, cnt, o);
             }
         }
-        if (STORE) {
+        if (STORE && lead) {
             R4<real> sf;
             sf.x = acc[0], sf.y = acc[1], sf.z = acc[2], sf.w = acc[3];
             R2<real> sm;
