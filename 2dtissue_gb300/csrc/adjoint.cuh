@@ -86,12 +86,14 @@ __device__ __forceinline__ int candidate_runs(const RepParams<real>& rp, const u
     const int id0 = key - rp.base;
     run[0] = make_int2(0, 0);
     if (id0 < rp.C) {
-        const uint4* dp = desc + (size_t)rp.desc_off + (size_t)id0 * 3;
-        const uint4 d0 = dp[0], d1 = dp[1], d2 = dp[2];
-        const unsigned e[9] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w, d2.x};
+        const uint4* dp = desc + (size_t)rp.desc_off + (size_t)id0 * 2;
+        const uint4 d0 = dp[0], d1 = dp[1];
+        const unsigned e[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
+        const int Lb = (int)((d0.x >> 2) & 1u), Rb = (int)((d0.x >> 3) & 1u);
 #pragma unroll
         for (int r = 0; r < 9; ++r) {
-            const int first = (int)(e[r] >> 4), len = (int)(e[r] & 3u);
+            const int first = r == 4 ? id0 - Lb : (int)(e[r < 4 ? r : r - 1] >> 4);
+            const int len = r == 4 ? 1 + Lb + Rb : (int)(e[r < 4 ? r : r - 1] & 3u);
             const int b0 = rp.base + first;
             const int t0 = len ? start[b0] : 0;
             const int t1 = len ? start[b0 + len] : 0;

@@ -222,32 +222,37 @@ void build_cell_level(const Mesh& m, double h, const double origin[3], CellLevel
 }
 
 void build_cell_descriptors(const CellLevel& L, std::vector<uint32_t>& desc) {
-    desc.assign((size_t)L.C * 12, 0u);
+    desc.assign((size_t)L.C * 8, 0u);
     for (int r = 0; r < L.gy * L.gz; ++r) {
         const int iy = r % L.gy, iz = r / L.gy;
         for (int k = 0; k < L.rows[2 * r + 1]; ++k) {
             const int* I = &L.ivals[4 * (L.rows[2 * r] + k)];
             for (int ix = I[0]; ix <= I[1]; ++ix) {
                 const int id = I[2] + ix - I[0];
+                int w = 0;
                 for (int e = 0; e < 9; ++e) {
                     const int dy = e % 3 - 1, dz = e / 3 - 1;
-                    if (iy + dy < 0 || iy + dy >= L.gy || iz + dz < 0 || iz + dz >= L.gz) continue;
-                    const int rr = (iz + dz) * L.gy + (iy + dy);
-                    int first = -1, fx = 0, lx = 0, len = 0;
-                    for (int q = 0; q < L.rows[2 * rr + 1]; ++q) {
-                        const int* J = &L.ivals[4 * (L.rows[2 * rr] + q)];
-                        const int lo = std::max(J[0], ix - 1), hi = std::min(J[1], ix + 1);
-                        if (lo > hi) continue;
-                        // ids are consecutive along the row; runs from two intervals are merged
-                        if (first < 0) first = J[2] + lo - J[0], fx = lo;
-                        len = (J[2] + hi - J[0]) - first + 1;
-                        lx = hi;
+                    int first = -1, len = 0;
+                    if (iy + dy >= 0 && iy + dy < L.gy && iz + dz >= 0 && iz + dz < L.gz) {
+                        const int rr = (iz + dz) * L.gy + (iy + dy);
+                        for (int q = 0; q < L.rows[2 * rr + 1]; ++q) {
+                            const int* J = &L.ivals[4 * (L.rows[2 * rr] + q)];
+                            const int lo = std::max(J[0], ix - 1), hi = std::min(J[1], ix + 1);
+                            if (lo > hi) continue;
+                            // ids are consecutive along the row; runs from two intervals are merged
+                            if (first < 0) first = J[2] + lo - J[0];
+                            len = (J[2] + hi - J[0]) - first + 1;
+                        }
                     }
-                    if (first >= 0) {
-                        desc[(size_t)id * 12 + e] = ((uint32_t)first << 4) | ((uint32_t)(fx - (ix - 1)) << 2) | (uint32_t)len;
-                        // word 9: bit e set when the run skips a non-surface cell (x -> id is not affine)
-                        if (lx - fx + 1 != len) desc[(size_t)id * 12 + 9] |= 1u << e;
+                    if (e == 4) {
+                        // the cell's own row: first = id - L, len = 1 + L + R, with L, R whether
+                        // x-1 and x+1 are surface cells; kept as two bits of word 0
+                        const int Lb = id - first, Rb = len - 1 - Lb;
+                        desc[(size_t)id * 8] |= ((uint32_t)Lb << 2) | ((uint32_t)Rb << 3);
+                        continue;
                     }
+                    if (first >= 0) desc[(size_t)id * 8 + w] |= ((uint32_t)first << 4) | (uint32_t)len;
+                    ++w;
                 }
             }
         }

@@ -52,9 +52,10 @@ struct CellLevel {
 void build_cell_level(const Mesh& m, double h, const double origin[3], CellLevel& L);
 
 // Per surface cell, the ids of its 27 neighbour cells as 9 x-runs (rows dy, dz in -1..1, in the
-// order r = (dz + 1) * 3 + (dy + 1)); entry = id of the run's first cell << 4 | (x offset of that
-// cell from ix - 1) << 2 | number of cells in the run (0..3); word 9 bit e is set when run e
-// skips a non-surface cell. 12 words per cell (2 spare).
+// order r = (dz + 1) * 3 + (dy + 1)), in 8 words (32 bytes, one sector): the 8 runs other than the
+// cell's own row, entry = id of the run's first cell << 4 | number of cells in the run (0..3);
+// the own row's run is the cell itself and its x-neighbours when they are surface cells (first =
+// id - L, length 1 + L + R, consecutive ids), with L and R in bits 2 and 3 of word 0.
 void build_cell_descriptors(const CellLevel& L, std::vector<uint32_t>& desc);
 
 

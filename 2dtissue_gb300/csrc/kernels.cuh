@@ -624,20 +624,24 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
         rep = (int)((unsigned)id >> a.local_bits);
         const RepParams<real>& rp = SINGLE ? a.rp0 : a.reps[rep];
 
-        // candidate ranges: the 9 x-runs of the particle's cell (static descriptors), as
-        // (first slot, count) pairs so that the loop switches runs with one 8-byte load
+        // candidate ranges: the 9 x-runs of the particle's cell (static 32-byte descriptors: 8 runs,
+        // the own row's derived from two bits; 48-byte descriptors with the 9th run stored took the
+        // step kernel 2% longer at 1M particles), as (first slot, count) pairs so that the loop
+        // switches runs with one 8-byte load
         __shared__ int2 s_run[9 * BLOCK];
         int2* srun = s_run + threadIdx.x;
         int nrun = 0;
         int total = 0;
         const int id0 = key0 - rp.base;
         if (id0 < rp.C) {
-            const uint4* dp = a.desc + (size_t)rp.desc_off + (size_t)id0 * 3;
-            const uint4 d0 = dp[0], d1 = dp[1], d2 = dp[2];
-            const unsigned e[9] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w, d2.x};
+            const uint4* dp = a.desc + (size_t)rp.desc_off + (size_t)id0 * 2;
+            const uint4 d0 = dp[0], d1 = dp[1];
+            const unsigned e[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
+            const int Lb = (int)((d0.x >> 2) & 1u), Rb = (int)((d0.x >> 3) & 1u);
 #pragma unroll
             for (int r = 0; r < 9; ++r) {
-                const int first = (int)(e[r] >> 4), len = (int)(e[r] & 3u);
+                const int first = r == 4 ? id0 - Lb : (int)(e[r < 4 ? r : r - 1] >> 4);
+                const int len = r == 4 ? 1 + Lb + Rb : (int)(e[r < 4 ? r : r - 1] & 3u);
                 const int b0 = rp.base + first;
                 const int t0 = len ? a.start[b0] : 0;
                 const int t1 = len ? a.start[b0 + len] : 0;
