@@ -129,6 +129,8 @@ struct tds_sim {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     // the whole run as one graph launch: conditional WHILE nodes around the steps (graph_steps 0)
     cudaGraphExec_t loop_graph = nullptr;
+    // a single step (tds_step / tds_step_async of one step) as one graph launch
+    cudaGraphExec_t step_graph = nullptr;
     int* loop_left = nullptr;  // device: [0] step blocks, [1] single steps left in the running loop graph
     int graph_steps = 0;         // 0: loop graph; 2..256 (even): steps per captured chunk (tuning)
     int step_block = 128;        // threads per k_step block (tuning: 128 or 256)
@@ -180,6 +182,10 @@ void free_graphs(tds_sim* s) {
     if (s->loop_graph) {
         cudaGraphExecDestroy(s->loop_graph);
         s->loop_graph = nullptr;
+    }
+    if (s->step_graph) {
+        cudaGraphExecDestroy(s->step_graph);
+        s->step_graph = nullptr;
     }
 }
 
@@ -697,6 +703,20 @@ int run_steps(tds_sim* s, int n, const double* noise_host, bool sync = true) {
             CK(cudaGraphLaunch(s->graph[c], s->stream));
             // graph_steps is even: the current buffer is the same after the chunk
             left -= s->graph_steps;
+        }
+        if (!s->timing && left == 1) {
+            // one step: the four kernels as one graph launch (fewer gaps between them than four
+            // stream launches)
+            if (!s->step_graph) {
+                cudaGraph_t g;
+                CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+                launch_one_step<real>(s, nullptr);
+                CK(cudaStreamEndCapture(s->stream, &g));
+                CK(cudaGraphInstantiate(&s->step_graph, g, 0));
+                cudaGraphDestroy(g);
+            }
+            CK(cudaGraphLaunch(s->step_graph, s->stream));
+            left = 0;
         }
         for (int k = 0; k < left; ++k) launch_one_step<real>(s, nullptr);
         CK(cudaGetLastError());
