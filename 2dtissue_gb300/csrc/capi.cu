@@ -105,7 +105,7 @@ struct tds_sim {
     double* series = nullptr;
     long long series_cap = 0;  // steps
     int* status = nullptr;
-    int* load_flag = nullptr;  // [0] the load in flight was refused, [1] a refused load not yet reported
+    int* load_flag = nullptr;  // [b] the load from input staging b was refused, [2] a refused load not yet reported
     long long* d_step = nullptr;
     int* packed_ids = nullptr;
     void* noise = nullptr;
@@ -359,7 +359,7 @@ int alloc_state(tds_sim* s) {
     if ((rc = dalloc(s, &s->tile_sum, (size_t)2 * s->n_tiles * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->phi_acc, (size_t)s->R * tdsk::kPhiCopies * 6 * sizeof(unsigned long long)))) return rc;
     if ((rc = dalloc(s, &s->status, sizeof(int)))) return rc;
-    if ((rc = dalloc(s, &s->load_flag, 2 * sizeof(int)))) return rc;
+    if ((rc = dalloc(s, &s->load_flag, 4 * sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->phi_pending, sizeof(int)))) return rc;
     if ((rc = dalloc(s, &s->d_step, sizeof(long long)))) return rc;
     if ((rc = dalloc(s, &s->loop_left, 2 * sizeof(int)))) return rc;
@@ -374,7 +374,7 @@ int alloc_state(tds_sim* s) {
     CK(cudaMemset(s->tile_sum, 0, (size_t)2 * s->n_tiles * sizeof(int)));
     CK(cudaMemset(s->phi_acc, 0, (size_t)s->R * tdsk::kPhiCopies * 6 * sizeof(unsigned long long)));
     CK(cudaMemset(s->status, 0, sizeof(int)));
-    CK(cudaMemset(s->load_flag, 0, 2 * sizeof(int)));
+    CK(cudaMemset(s->load_flag, 0, 4 * sizeof(int)));
     CK(cudaMemset(s->phi_pending, 0, sizeof(int)));
     const int nN = s->N;
     CK(cudaMemcpy(s->start + s->M, &nN, sizeof(int), cudaMemcpyHostToDevice));
@@ -774,36 +774,37 @@ struct Carve {
 int take_refused_load(tds_sim* s, const char* who) {
     // on the handle's (non-blocking) stream, so that the clear is ordered before any later load
     int refused = 0;
-    CK(cudaMemcpyAsync(&refused, s->load_flag + 1, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(&refused, s->load_flag + 2, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     if (!refused) return TDS_OK;
-    CK(cudaMemsetAsync(s->load_flag + 1, 0, sizeof(int), s->stream));
+    CK(cudaMemsetAsync(s->load_flag + 2, 0, sizeof(int), s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return fail(s, TDS_ERR_ARG, std::string(who) + ": face index out of range; the load was refused and the "
                                                    "state is the one before it");
 }
 
-// The face indices are checked on the device (k_check_faces, when check_faces) rather than by a
-// host loop over the caller's array: the host loop took ~0.23 ms of host time per call at 1M
-// particles, about as long as the whole pipelined step. A refused load changes nothing.
+// The face indices are checked on the device (k_check_faces) rather than by a host loop over the
+// caller's array (the host loop took ~0.23 ms of host time per call at 1M particles, about as long
+// as the whole pipelined step): on the upload stream, right after the upload, so that the check
+// is off the compute stream's chain (load_state); its verdict for staging b is load_flag[b]. A
+// refused load changes nothing.
 template <typename real, typename I = double>
-int load_from_staging(tds_sim* s, int b, bool has_face, bool has_r3d, bool sync, bool check_faces) {
+int load_from_staging(tds_sim* s, int b, bool has_face, bool has_r3d, bool sync, bool checked) {
     const size_t N = (size_t)s->N;
     s->cur = 0;
     const int nb = (s->N + 255) / 256;
     const I* in = reinterpret_cast<const I*>(s->in_d[b]);
-    CK(cudaMemsetAsync(s->load_flag, 0, sizeof(int), s->stream));
-    if (has_face && check_faces)
-        tdsk::k_check_faces<<<nb, 256, 0, s->stream>>>(s->in_i[b], s->N, s->mesh->t.F, s->load_flag);
+    int* flag = s->load_flag + b;
+    if (!checked) CK(cudaMemsetAsync(flag, 0, sizeof(int), s->stream));
     const int nc = (int)std::min<long long>((s->M + 255) / 256, 8 * 152);
-    tdsk::k_clear_counts<<<nc, 256, 0, s->stream>>>(s->count, s->M, s->tile_sum, 2 * s->n_tiles, s->load_flag);
+    tdsk::k_clear_counts<<<nc, 256, 0, s->stream>>>(s->count, s->M, s->tile_sum, 2 * s->n_tiles, flag);
     tdsk::k_load_state<real, I><<<nb, 256, 0, s->stream>>>(
         in, in + 2 * N, s->in_i[b], in + 3 * N, has_face, has_r3d, (const real*)s->rec, s->adj, s->G,
         s->bin_start, s->bin_faces, (const RepParams<real>*)s->reps, s->local_bits, s->rows, s->ivals, s->ids[0],
         (R4<real>*)s->pos[0], (R4<real>*)s->pol[0], (R2<real>*)s->uv[0], s->ids[0], (R2<real>*)s->vel[0], s->cnt[0],
-        s->key[0], s->count, s->N, s->status, s->load_flag);
+        s->key[0], s->count, s->N, s->status, flag);
     tdsk::k_tile_sums<<<s->n_tiles, tdsk::kScanThreads, 0, s->stream>>>(s->count, s->M, s->tile_sum, s->n_tiles,
-                                                                         s->d_step, s->load_flag);
+                                                                         s->d_step, flag);
     CK(cudaGetLastError());
     CK(cudaEventRecord(s->ev_in_free[b], s->stream));
     if (!sync) return TDS_OK;
@@ -831,6 +832,10 @@ int load_state(tds_sim* s, const View* in, bool sync) {
     CK(cudaMemcpyAsync(d_th, in->theta, N * sizeof(I), cudaMemcpyHostToDevice, s->up));
     if (in->face) CK(cudaMemcpyAsync(d_face, in->face, N * sizeof(int), cudaMemcpyHostToDevice, s->up));
     if (in->r3d) CK(cudaMemcpyAsync(d_r3, in->r3d, 3 * N * sizeof(I), cudaMemcpyHostToDevice, s->up));
+    CK(cudaMemsetAsync(s->load_flag + b, 0, sizeof(int), s->up));
+    if (in->face)
+        tdsk::k_check_faces<<<(s->N + 255) / 256, 256, 0, s->up>>>(d_face, s->N, s->mesh->t.F, s->load_flag + b,
+                                                                   s->load_flag + 2);
     CK(cudaEventRecord(s->ev_in_ready[b], s->up));
     CK(cudaStreamWaitEvent(s->stream, s->ev_in_ready[b], 0));
     return load_from_staging<real, I>(s, b, in->face != nullptr, in->r3d != nullptr, sync, true);

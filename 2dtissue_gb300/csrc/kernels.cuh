@@ -1143,15 +1143,15 @@ __global__ void k_pack_particles(const R4<real>* pos, const R2<real>* uv, const 
 }
 
 // A state load is checked on the device before anything of the current state is touched: a face
-// index >= F refuses the whole load (flag[0], cleared before each load) and records the refusal
-// for the caller (flag[1], sticky until reported); negative indices mean "locate" and are valid.
-// The kernels of the load then leave the state, the cell counts and the tile counts as they were.
-__global__ void k_check_faces(const int* __restrict__ face, int N, int F, int* flag) {
+// index >= F refuses the whole load (refused, cleared before each check) and records the refusal
+// for the caller (sticky, until reported); negative indices mean "locate" and are valid. The
+// kernels of the load then leave the state, the cell counts and the tile counts as they were.
+__global__ void k_check_faces(const int* __restrict__ face, int N, int F, int* refused, int* sticky) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool bad = i < N && face[i] >= F;
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) {
-        atomicOr(&flag[0], 1);
-        atomicOr(&flag[1], 1);
+        atomicOr(refused, 1);
+        atomicOr(sticky, 1);
     }
 }
 // zeroes the cell counts and both parities of the tile counts before a load (unless refused)
