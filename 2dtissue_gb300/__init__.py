@@ -387,8 +387,8 @@ class Simulation:
         spec = _AdjSpec(int(n_steps), int(checkpoint_stride), _ptr(tgt), float(w_pos), _ptr(phi), float(w_phi),
                         int(window), int(gather_lanes))
         dp = np.zeros((R, 8))
-        duv = np.zeros((N, 2))
-        dth = np.zeros(N)
+        duv = np.empty((N, 2))  # written in full by the library
+        dth = np.empty(N)
         res = _AdjResult(0.0, _ptr(dp), _ptr(duv), _ptr(dth), 0)
         self._check(lib().tds_adjoint_run(self.h, C.byref(spec), C.byref(res)))
         return dict(loss=res.loss, d_params=dp[:, :7], d_uv0=duv, d_theta0=dth, checkpoint_stride=res.checkpoint_stride)

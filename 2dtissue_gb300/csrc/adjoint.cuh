@@ -528,6 +528,43 @@ __global__ void k_adj_phib(const double* phisum, const double* phibar, const Rep
     out[e] = o;
 }
 
+// Position term of the loss per replica: sum over the replica's particles of |r_T - r*|^2 in FP64
+// (the final state by slot: a replica's slots are off[r] .. off[r] + cnt[r] - 1; the target by
+// particle index), in a fixed order (one block per replica, a fixed tree).
+template <typename real>
+__global__ void k_adj_pos_loss(const R4<real>* pos, const int* ids, const RepParams<real>* reps, int local_bits,
+                               const double* tgt, const int* off, const int* cnt, double* out) {
+    __shared__ double s[256];
+    const int r = blockIdx.x;
+    double acc = 0;
+    for (int q = off[r] + threadIdx.x; q < off[r] + cnt[r]; q += 256) {
+        const unsigned id = (unsigned)ids[q];
+        const size_t gid = (size_t)(reps[id >> local_bits].off + (int)(id & ((1u << local_bits) - 1u)));
+        const R4<real> P = pos[q];
+        const double dx = (double)P.x - tgt[3 * gid], dy = (double)P.y - tgt[3 * gid + 1];
+        const double dz = (double)P.z - tgt[3 * gid + 2];
+        acc += dx * dx + dy * dy + dz * dz;
+    }
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[r] = s[0];
+}
+
+// The adjoint of the initial state, (u, v, theta) padded to 4 reals by particle index, as the
+// caller's double arrays: d_uv [2N], d_theta [N].
+template <typename real>
+__global__ void k_adj_out(const real* lam, double* d_uv, double* d_th, int N) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const R4<real> l = reinterpret_cast<const R4<real>*>(lam)[i];
+    d_uv[2 * (size_t)i] = (double)l.x, d_uv[2 * (size_t)i + 1] = (double)l.y;
+    d_th[i] = (double)l.z;
+}
+
 // Per-replica sums of the per-slot parameter terms (replica r: slots off[r] .. off[r] + cnt[r] - 1),
 // in a fixed order (one block per replica).
 template <typename real>

@@ -1154,7 +1154,7 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     R4<real>*aF = nullptr, *aM = nullptr, *aP = nullptr;
     real* gpar = nullptr;
     R4<real>* dSb = nullptr;  // dL/dS per stored step and replica (k_adj_phib)
-    double *phisum = nullptr, *phibar = nullptr, *rtgt = nullptr, *d_gp = nullptr;
+    double *phisum = nullptr, *phibar = nullptr, *rtgt = nullptr, *d_gp = nullptr, *d_ploss = nullptr;
     int *d_off = nullptr, *d_cnt = nullptr, *d_t0 = nullptr;
     // all work buffers come from one block: measured first, then carved
     auto carve = [&](Carve& A) -> bool {
@@ -1174,10 +1174,11 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
         phibar = A.get<double>((size_t)T * R);
         dSb = A.get<R4<real>>((size_t)T * R);
         rtgt = sp->r3d_target ? A.get<double>(3 * N) : nullptr;
+        d_ploss = A.get<double>(R);
         d_off = A.get<int>(R), d_cnt = A.get<int>(R), d_t0 = A.get<int>(1);
         d_gp = A.get<double>(R * tdsk::kGPar);
         return ok && lam[0] && lam[1] && aF && aM && aP && gpar && phisum && phibar && dSb && d_off && d_cnt && d_t0 &&
-               d_gp &&
+               d_gp && d_ploss &&
                (!sp->r3d_target || rtgt);
     };
     {
@@ -1204,6 +1205,15 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     }
     if ((rc = ensure_series(s, s->step + T))) return rc;
     free_graphs(s);
+    {
+        // replica slot ranges (the per-replica sums) and the position target, uploaded before the run
+        std::vector<int> off(s->off.begin(), s->off.end()), cnt(s->n_rep.begin(), s->n_rep.end());
+        CK(cudaMemcpyAsync(d_off, off.data(), R * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(d_cnt, cnt.data(), R * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+        if (rtgt)
+            CK(cudaMemcpyAsync(rtgt, sp->r3d_target, 3 * N * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
 
     // ---- forward: checkpoints every K steps, the last segment stored step by step ----
     const long long t_base = s->step;
@@ -1237,23 +1247,17 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     snapshot_copy<real>(s, fin, true);
     if ((rc = sync_all(s))) return rc;
 
-    // ---- loss (host, double) ----
+    // ---- loss (double): the position term per replica on the device, the order-parameter term here ----
     double loss = 0;
     std::vector<double> phib((size_t)T * R, 0.0);
     if (sp->r3d_target && sp->w_pos > 0) {
-        std::vector<double> r3(3 * N);
-        tds_state_view v = {nullptr, nullptr, nullptr, r3.data(), nullptr, nullptr};
-        if ((rc = save_state<real>(s, &v, true))) return rc;
-        for (size_t r = 0; r < R; ++r) {
-            double acc = 0;
-            for (int i = s->off[r]; i < s->off[r] + s->n_rep[r]; ++i)
-                for (int k = 0; k < 3; ++k) {
-                    const double d = r3[3 * (size_t)i + k] - sp->r3d_target[3 * (size_t)i + k];
-                    acc += d * d;
-                }
-            loss += sp->w_pos * acc / s->n_rep[r];
-        }
-        CK(cudaMemcpyAsync(rtgt, sp->r3d_target, 3 * N * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+        tdsk::k_adj_pos_loss<real><<<(int)R, 256, 0, s->stream>>>((const R4<real>*)s->pos[s->cur], s->ids[s->cur],
+                                                                  (const RepParams<real>*)s->reps, s->local_bits,
+                                                                  rtgt, d_off, d_cnt, d_ploss);
+        std::vector<double> pl(R);
+        CK(cudaMemcpyAsync(pl.data(), d_ploss, R * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (size_t r = 0; r < R; ++r) loss += sp->w_pos * pl[r] / s->n_rep[r];
     }
     const bool phi_term = sp->phi_target && sp->w_phi > 0;
     if (phi_term) {
@@ -1268,13 +1272,6 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
             }
         CK(cudaMemcpyAsync(phibar, phib.data(), phib.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
     }
-    {
-        std::vector<int> off(s->off.begin(), s->off.end()), cnt(s->n_rep.begin(), s->n_rep.end());
-        CK(cudaMemcpyAsync(d_off, off.data(), R * sizeof(int), cudaMemcpyHostToDevice, s->stream));
-        CK(cudaMemcpyAsync(d_cnt, cnt.data(), R * sizeof(int), cudaMemcpyHostToDevice, s->stream));
-        CK(cudaStreamSynchronize(s->stream));
-    }
-
     // ---- reverse sweep ----
     Range rev("adjoint reverse");
     CK(cudaMemsetAsync(lam[0], 0, 4 * N * sizeof(real), s->stream));
@@ -1404,19 +1401,24 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     tdsk::k_adj_reduce<real><<<(int)R, 256, 0, s->stream>>>(gpar, (long long)N, d_off, d_cnt, d_gp);
     CK(cudaGetLastError());
     snapshot_copy<real>(s, fin, false);  // the handle ends where the forward ended
-    std::vector<real> lh(4 * N);
     std::vector<double> gh(R * tdsk::kGPar);
-    CK(cudaMemcpyAsync(lh.data(), lam[T & 1], 4 * N * sizeof(real), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaMemcpyAsync(gh.data(), d_gp, gh.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    if (res->d_uv0 || res->d_theta0) {
+        // the initial state's adjoint as the caller's doubles, converted on the device into the
+        // output staging (8N doubles) and copied straight into the caller's arrays
+        double* d_uv = s->st_d[0];
+        double* d_th = d_uv + 2 * N;
+        tdsk::k_adj_out<real><<<(unsigned)((N + 255) / 256), 256, 0, s->stream>>>(lam[T & 1], d_uv, d_th, (int)N);
+        if (res->d_uv0)
+            CK(cudaMemcpyAsync(res->d_uv0, d_uv, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        if (res->d_theta0)
+            CK(cudaMemcpyAsync(res->d_theta0, d_th, N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    }
     if ((rc = sync_all(s))) return rc;
     res->loss = pre_loss + loss;
     res->checkpoint_stride = K;
     if (res->d_params)
         for (size_t i = 0; i < gh.size(); ++i) res->d_params[i] = gh[i];
-    for (size_t i = 0; i < N; ++i) {
-        if (res->d_uv0) res->d_uv0[2 * i] = (double)lh[4 * i], res->d_uv0[2 * i + 1] = (double)lh[4 * i + 1];
-        if (res->d_theta0) res->d_theta0[i] = (double)lh[4 * i + 2];
-    }
     return TDS_OK;
 }
 
