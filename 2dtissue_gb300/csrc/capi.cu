@@ -1109,8 +1109,6 @@ int adjoint_run(tds_sim* s, const tds_adjoint_spec* sp_in, tds_adjoint_result* r
     const int T = sp->n_steps;
     const size_t N = (size_t)s->N, M = (size_t)s->M, R = (size_t)s->R;
     const size_t b_state = N * (2 * sizeof(R4<real>) + sizeof(R2<real>) + 2 * sizeof(int));
-    // the stored steps keep their pair sums (24 B per particle in FP32) when the step kernel runs one
-    // lane per particle (with more lanes its sums round differently from the reverse step's loop)
     // a stored step keeps its pair sums (24 B per particle in FP32), as the step kernel computed them
     const size_t b_store = b_state + (M + 1) * sizeof(int) + N * (sizeof(R4<real>) + sizeof(R2<real>));
     const size_t b_snap = b_state + M * sizeof(int) + 2 * (size_t)s->n_tiles * sizeof(int) + 64;
