@@ -214,8 +214,8 @@ def test_injected_noise_matches_philox(tg, mesh_l4, orc):
 
 def test_graph_and_direct_launches_agree(tg, mesh_l4):
     """The loop graph (one launch per run, the step count set on the device), graphs of 16 steps
-    and direct launches give the same states and order-parameter series, bit for bit, over runs of
-    different lengths on the same handle."""
+    with direct launches for the rest, and one-step graphs give the same states and
+    order-parameter series, bit for bit, over runs of different lengths on the same handle."""
     runs = [37, 2, 3, 16, 1, 25]
     a = tg.Simulation(mesh_l4, tg.Params(), 500, seed=1)
     c = tg.Simulation(mesh_l4, tg.Params(), 500, seed=1,
@@ -226,9 +226,9 @@ def test_graph_and_direct_launches_agree(tg, mesh_l4):
         x.start()
     for n in runs:
         a.step(n)  # the loop graph for n >= 2
-        c.step(n)  # chunks of 16 steps + direct launches
+        c.step(n)  # chunks of 16 steps + direct launches (a remainder of one: the one-step graph)
         for _ in range(n):
-            b.step(1)
+            b.step(1)  # the one-step graph
         sa, sb, sc = a.get_state(), b.get_state(), c.get_state()
         for k in sa:
             np.testing.assert_array_equal(sa[k], sb[k])
