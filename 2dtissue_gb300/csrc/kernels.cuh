@@ -121,7 +121,7 @@ struct StepArgs {
     unsigned long long seed;
     int* status;
     int N;
-    int single;  // one replica: pc0 holds its pair constants
+    int single;  // every replica has the same pair constants, held in pc0
     PairC<real> pc0;
     RepParams<real> rp0;  // the replica's parameters when there is one (read from the constant bank)
     int* nbr_list;  // neighbour export (the NBR instantiation only): nbr_cap ids per particle
