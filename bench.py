@@ -788,11 +788,11 @@ PROFILE_TUNING = dict(cells_per_particle=4.0, step_block=128, graph_steps=16, la
 
 def run_profile(args):
     """Minimal driver for ncu: the 1M-particle system, `warmup` steps, then `steps` steps (graphs of
-    16 steps); no timing."""
+    16 steps; `--lanes` lanes per particle); no timing."""
     import torch
     tg = importlib.import_module("2dtissue_gb300")
     mesh, p, n, _ = workload_1m(tg)
-    sim = tg.Simulation(mesh, p, n, seed=0, precision=32, tuning=PROFILE_TUNING)
+    sim = tg.Simulation(mesh, p, n, seed=0, precision=32, tuning=dict(PROFILE_TUNING, lanes_per_particle=args.lanes))
     sim.start()
     sim.step(args.warmup)
     sim.step_async(args.steps)
@@ -854,6 +854,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--plain-only", action="store_true", help="only the headline plain-step leg")
+    ap.add_argument("--lanes", type=int, default=1, choices=[1, 2, 4],
+                    help="with --profile (plain workload): lanes per particle of the step kernel")
     ap.add_argument("--profile", action="store_true", help="only run warmup + steps (for ncu)")
     ap.add_argument("--e2e", action="store_true", help="with --profile: steps iterations of the end-to-end loop")
     ap.add_argument("--workload", default="plain", choices=["plain", "ensemble", "adjoint", "adjoint_batched", "ref"])
