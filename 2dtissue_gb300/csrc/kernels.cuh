@@ -500,9 +500,10 @@ __device__ __forceinline__ void pair_term(const RepParams<real>& rp, const R4<re
 // NBR (a test hook's instantiation): each neighbour's sorted slot is also written to list[0..cap).
 // SPEC: both candidates' polarities are loaded with their positions, before the distance tests (one
 // dependent load level per iteration instead of two, at the cost of loading non-neighbours'
-// polarities): the single-system step kernel at 1M particles 109.4 -> 107.2 us, at 10,000
-// particles 21.5 -> 20.6 us per step; on the 6.75M-particle ensemble, whose state does not stay
-// in L2, 571 -> 576 us, so the ensemble kernel keeps the loads behind the tests.
+// polarities). Used when the pair constants come from the kernel parameters (one replica, or
+// replicas that share them): 1M particles 109.4 -> 107.2 us, 10,000 particles 21.5 -> 20.6 us
+// per step, the 4,096-replica ensemble 559 -> 547 us; with per-replica constants from the table
+// (five more live registers) the loads stay behind the tests.
 template <typename real, int BLOCK, bool NBR = false, bool SPEC = false>
 __device__ __forceinline__ void pair_sums_s(const PairC<real>& pc, const R4<real>& P, const R4<real>* __restrict__ pos,
                                           const R4<real>* __restrict__ pol, const int2* srun, int total, int self,
@@ -660,8 +661,8 @@ __global__ void __launch_bounds__(BLOCK, (sizeof(real) == 4 ? 6 : 3) * 256 / BLO
                         : nullptr;
         if (LPP == 1) {
             if (a.single)
-                pair_sums_s<real, BLOCK, NBR, SINGLE>(a.pc0, P, a.pos, a.pol, srun, total, q, acc, cnt, list,
-                                                      a.nbr_cap);
+                pair_sums_s<real, BLOCK, NBR, true>(a.pc0, P, a.pos, a.pol, srun, total, q, acc, cnt, list,
+                                                    a.nbr_cap);
             else
                 pair_sums_s<real, BLOCK, NBR>(pair_constants(rp), P, a.pos, a.pol, srun, total, q, acc, cnt, list,
                                               a.nbr_cap);
