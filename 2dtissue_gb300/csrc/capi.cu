@@ -427,8 +427,11 @@ int ensure_series(tds_sim* s, long long steps_needed) {
 
 cudaEvent_t take_event(tds_sim* s) {
     if (s->ev_pool.empty()) {
-        cudaEvent_t e;
-        cudaEventCreate(&e);
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;  // the launch goes untimed
+        }
         return e;
     }
     cudaEvent_t e = s->ev_pool.back();
@@ -442,17 +445,17 @@ struct KernelTimer {
     int k;
     cudaEvent_t a = nullptr;
     KernelTimer(tds_sim* s_, int k_) : s(s_), k(k_) {
-        if (s->timing) {
-            a = take_event(s);
-            cudaEventRecord(a, s->stream);
-        }
+        if (s->timing && (a = take_event(s))) cudaEventRecord(a, s->stream);
     }
     ~KernelTimer() {
-        if (s->timing) {
-            cudaEvent_t b = take_event(s);
-            cudaEventRecord(b, s->stream);
-            s->ev_pending.push_back({k, {a, b}});
+        if (!a) return;
+        cudaEvent_t b = take_event(s);
+        if (!b) {
+            s->ev_pool.push_back(a);
+            return;
         }
+        cudaEventRecord(b, s->stream);
+        s->ev_pending.push_back({k, {a, b}});
     }
 };
 

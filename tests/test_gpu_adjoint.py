@@ -327,3 +327,31 @@ def test_adjoint_with_lanes_per_particle(tg, orc, mesh_l4, adj_setup, lanes):
     gpu = res["d_params"][0] @ direction + (res["d_uv0"] * duv).sum() + res["d_theta0"] @ dth
     np.testing.assert_allclose(res["loss"], loss, rtol=1e-9)
     np.testing.assert_allclose(gpu, dloss, rtol=1e-6)
+
+
+def test_kernel_timing_changes_no_result(tg, mesh_l4):
+    """With per-kernel timing on, steps and the adjoint's segments launch kernel by kernel between
+    CUDA events instead of as graphs: the same state and gradients bit for bit, and every launch of
+    the four step kernels counted."""
+    outs = []
+    for timing in (False, True):
+        sim = _start(tg, mesh_l4, 32)
+        s0 = sim.get_state()
+        sim.kernel_timing(timing)
+        sim.step(5)
+        sim.step(1)
+        r = sim.adjoint(T + 3, r3d_target=s0["r3d"], w_pos=1.0, phi_target=np.zeros(T + 3), w_phi=1.0,
+                        checkpoint_stride=4)
+        outs.append((sim.get_state(), r))
+        if timing:
+            kt = sim.kernel_times()
+            n = kt["step"][1]
+            # 6 plain steps, the forward's T + 3 and the recompute of the two earlier segments
+            assert n == 6 + (T + 3) + 8
+            assert kt["scan"][1] == kt["scatter"][1] == kt["order"][1] == n
+            assert all(ms > 0 for ms, c in kt.values() if c)
+        sim.close()
+    for k in ("uv", "theta", "face", "r3d"):
+        np.testing.assert_array_equal(outs[0][0][k], outs[1][0][k])
+    for k in ("loss", "d_params", "d_uv0", "d_theta0"):
+        np.testing.assert_array_equal(outs[0][1][k], outs[1][1][k])
