@@ -804,7 +804,7 @@ int take_refused_load(tds_sim* s, const char* who) {
 // The face indices are checked on the device (k_check_faces) rather than by a host loop over the
 // caller's array (the host loop took ~0.23 ms of host time per call at 1M particles, about as long
 // as the whole pipelined step): on the upload stream, right after the upload, so that the check
-// is off the compute stream's chain (load_state); its verdict for staging b is load_flag[b]. A
+// is off the compute stream's chain (load_state); its outcome for staging b is load_flag[b]. A
 // refused load changes nothing.
 template <typename real, typename I = double>
 int load_from_staging(tds_sim* s, int b, bool has_face, bool has_r3d, bool sync, bool checked) {
