@@ -64,3 +64,18 @@ def place_particles(orc_mesh, arrays, n, seed):
     r3 = np.array([orc_mesh.map(f[i], *p[i]) for i in range(n)])
     th = rng.random(n) * 2 * np.pi - np.pi
     return dict(uv=p, theta=th, face=f.astype(np.int32), r3d=r3, ids=np.arange(n, dtype=np.int32))
+
+
+def face_map_residual(arrays, uv, face, r3d):
+    """Per particle: the smallest barycentric coordinate of its chart position in its face's chart
+    triangle, and the distance from its 3D position to the face's chart map of that position."""
+    fuv, f3 = arrays["fuv"][face], arrays["f3"][face]
+    a, b, c = (arrays["uv"][fuv[:, k]] for k in range(3))
+    e1, e2, d = b - a, c - a, uv - a
+    det = e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0]
+    w1 = (d[:, 0] * e2[:, 1] - d[:, 1] * e2[:, 0]) / det
+    w2 = (e1[:, 0] * d[:, 1] - e1[:, 1] * d[:, 0]) / det
+    w0 = 1 - w1 - w2
+    v = arrays["v3"]
+    r = w0[:, None] * v[f3[:, 0]] + w1[:, None] * v[f3[:, 1]] + w2[:, None] * v[f3[:, 2]]
+    return np.minimum(np.minimum(w0, w1), w2), np.linalg.norm(r - r3d, axis=1)

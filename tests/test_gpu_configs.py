@@ -22,7 +22,9 @@ import importlib
 import numpy as np
 import pytest
 
-from conftest import get_mesh, oracle_mesh
+from scipy.spatial import cKDTree
+
+from conftest import face_map_residual, get_mesh, oracle_mesh
 from test_gpu_parity import compare_step
 
 pytestmark = pytest.mark.gpu
@@ -150,6 +152,26 @@ def test_ragged_ensemble_4096_replicas_parity(tg, orc):
                            local_bits=lb, centroid=cen)
         np.testing.assert_allclose(phi[3, r], np.linalg.norm(out["phi_sums"][:3]) / ns[r], rtol=1e-4, atol=1e-6)
         np.testing.assert_allclose(psi[3, r], np.linalg.norm(out["phi_sums"][3:]) / ns[r], rtol=1e-4, atol=1e-6)
+    # the whole 6.75M-particle ensemble: every neighbour count against a k-d tree over the step's
+    # starting positions (replicas set 100 apart along x, so that no pair crosses replicas; the
+    # mesh spans 8 along x), particles with a pair within 1e-5 of r_max excepted; every 3D
+    # position is its face's chart map of its chart position, inside that face
+    rep = np.repeat(np.arange(len(ns)), ns)
+    r0 = g0["r3d"]
+    shifted = r0 + np.outer(100.0 * rep, [1.0, 0.0, 0.0])
+    tree = cKDTree(shifted)
+    cnt = tree.query_ball_point(shifted, 0.12, return_length=True, workers=-1) - 1
+    off_ = np.nonzero(cnt != g1["nbr"])[0]
+    if len(off_):
+        pairs = tree.query_pairs(0.12 + 1e-4, output_type="ndarray")
+        d = np.linalg.norm(r0[pairs[:, 0]] - r0[pairs[:, 1]], axis=1)
+        band = np.zeros(len(r0), bool)
+        band[pairs[np.abs(d - 0.12) < 1e-5].ravel()] = True
+        assert np.all(band[off_]), off_[~band[off_]][:10]
+    assert len(off_) <= 1e-5 * len(r0)
+    wmin, res = face_map_residual(arr, g1["uv"], g1["face"], g1["r3d"])
+    assert wmin.min() > -1e-3
+    assert res.max() < 1e-4  # coordinates up to 4
     sim.close()
 
 

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 from scipy.spatial import cKDTree
 
-from conftest import get_mesh, oracle_mesh
+from conftest import face_map_residual, get_mesh, oracle_mesh
 
 pytestmark = pytest.mark.gpu
 
@@ -141,21 +141,6 @@ def params_1m(tg, mesh):
     return N, tg.Params(radius=R, r_max=2.4 * R, eta=0.3, dt=0.01)
 
 
-def face_map_residual(arrays, uv, face, r3d):
-    """Per particle: the smallest barycentric coordinate of its chart position in its face's chart
-    triangle, and the distance from its 3D position to the face's chart map of that position."""
-    fuv, f3 = arrays["fuv"][face], arrays["f3"][face]
-    a, b, c = (arrays["uv"][fuv[:, k]] for k in range(3))
-    e1, e2, d = b - a, c - a, uv - a
-    det = e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0]
-    w1 = (d[:, 0] * e2[:, 1] - d[:, 1] * e2[:, 0]) / det
-    w2 = (e1[:, 0] * d[:, 1] - e1[:, 1] * d[:, 0]) / det
-    w0 = 1 - w1 - w2
-    v = arrays["v3"]
-    r = w0[:, None] * v[f3[:, 0]] + w1[:, None] * v[f3[:, 1]] + w2[:, None] * v[f3[:, 2]]
-    return np.minimum(np.minimum(w0, w1), w2), np.linalg.norm(r - r3d, axis=1)
-
-
 def test_1m_particle_full_state_invariants(tg):
     """Size-independent properties of the whole 1,048,576-particle FP32 state after a step: every
     neighbour count is the number of particles within r_max of the particle at the step's start
@@ -171,7 +156,7 @@ def test_1m_particle_full_state_invariants(tg):
     sim.step(1)
     g1 = sim.get_state()
     r0 = g0["r3d"]
-    cnt = cKDTree(r0).query_ball_point(r0, p.r_max, return_length=True) - 1
+    cnt = cKDTree(r0).query_ball_point(r0, p.r_max, return_length=True, workers=-1) - 1
     off = np.nonzero(cnt != g1["nbr"])[0]
     band = cutoff_band(r0, p.r_max)
     assert np.all(band[off]), off[~band[off]][:10]
