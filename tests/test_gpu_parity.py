@@ -34,9 +34,24 @@ def cutoff_band(r3d, r_max, eps=BAND):
     return out
 
 
+def edge_distance(om, f, p):
+    """Distance in the chart from point p to the nearest edge of face f's chart triangle."""
+    tri = om.uv[om.fuv[f]]
+    best = np.inf
+    for k in range(3):
+        a, b = tri[k], tri[(k + 1) % 3]
+        t = np.clip(np.dot(p - a, b - a) / np.dot(b - a, b - a), 0.0, 1.0)
+        best = min(best, float(np.linalg.norm(p - (a + t * (b - a)))))
+    return best
+
+
 def compare_step(orc, om, params, g0, g1, step, seed, precision, subset=None, ids=None, local_bits=31,
-                 centroid=(0, 0, 0)):
-    """g0: GPU state before the step (id order), g1: after. Returns the oracle output."""
+                 centroid=(0, 0, 0), tally=None):
+    """g0: GPU state before the step (id order), g1: after. Returns the oracle output.
+    tally (a dict): instead of asserting the value tolerances, add to tally[name] the number of
+    compared particles outside the tolerance of each value (uv, r3d, cos/sin theta, vel_uv), to
+    tally["worst"] the largest deviation in units of the tolerance and to tally["n"] the number
+    of particles compared; neighbour counts and faces are asserted either way."""
     n = len(g0["theta"])
     st = dict(uv=g0["uv"], theta=g0["theta"], face=g0["face"], r3d=g0["r3d"],
               ids=np.arange(n, dtype=np.int32) if ids is None else ids)
@@ -47,22 +62,32 @@ def compare_step(orc, om, params, g0, g1, step, seed, precision, subset=None, id
     ok = ~amb
     # neighbour counts: exact outside the band
     np.testing.assert_array_equal(g1["nbr"][sel][ok], out["nbr"][ok])
-    # faces: exact unless the point sits on a shared edge / vertex
+    # faces: exact unless the point sits on a shared edge / vertex (the oracle's locate reports
+    # it, or the new chart position is within 1e-6 of an edge of either face)
     fmis = np.where(g1["face"][sel] != out["face"])[0]
     for k in fmis:
         i = sel[k]
         f, mode = om.locate(*g1["uv"][i], int(g1["face"][i]))
-        assert f == g1["face"][i] or mode != 0, "face mismatch away from an edge for particle %d" % i
+        near = min(edge_distance(om, int(g1["face"][i]), g1["uv"][i]), edge_distance(om, int(out["face"][k]), out["uv"][k]))
+        assert f == g1["face"][i] or mode != 0 or near < 1e-6, "face mismatch away from an edge for particle %d" % i
     assert len(fmis) <= max(2, 1e-3 * len(sel))
     good = ok.copy()
     good[fmis] = False
-    np.testing.assert_allclose(g1["uv"][sel][good], out["uv"][good], **tol)
-    np.testing.assert_allclose(g1["r3d"][sel][good], out["r3d"][good],
-                               rtol=tol["rtol"], atol=tol["atol"] * max(1.0, np.abs(out["r3d"]).max()))
-    np.testing.assert_allclose(np.cos(g1["theta"][sel][good]), np.cos(out["theta"][good]), **tol)
-    np.testing.assert_allclose(np.sin(g1["theta"][sel][good]), np.sin(out["theta"][good]), **tol)
-    np.testing.assert_allclose(g1["vel_uv"][sel][good], out["vel_uv"][good],
-                               rtol=tol["rtol"] * 10, atol=tol["atol"] * 10)
+    r3d_atol = tol["atol"] * max(1.0, np.abs(out["r3d"]).max())
+    checks = [("uv", g1["uv"][sel], out["uv"], tol["rtol"], tol["atol"]),
+              ("r3d", g1["r3d"][sel], out["r3d"], tol["rtol"], r3d_atol),
+              ("cos", np.cos(g1["theta"][sel]), np.cos(out["theta"]), tol["rtol"], tol["atol"]),
+              ("sin", np.sin(g1["theta"][sel]), np.sin(out["theta"]), tol["rtol"], tol["atol"]),
+              ("vel_uv", g1["vel_uv"][sel], out["vel_uv"], tol["rtol"] * 10, tol["atol"] * 10)]
+    if tally is None:
+        for name, gpu, ref, rtol, atol in checks:
+            np.testing.assert_allclose(gpu[good], ref[good], rtol=rtol, atol=atol, err_msg=name)
+        return out
+    tally["n"] = tally.get("n", 0) + int(good.sum())
+    for name, gpu, ref, rtol, atol in checks:
+        d = (np.abs(gpu - ref) / (atol + rtol * np.abs(ref))).reshape(len(ref), -1).max(1)[good]
+        tally[name] = tally.get(name, 0) + int((d > 1).sum())
+        tally["worst"] = max(tally.get("worst", 0.0), float(d.max(initial=0.0)))
     return out
 
 
