@@ -178,6 +178,24 @@ def test_ragged_ensemble_4096_replicas_parity(tg, orc):
         np.testing.assert_allclose(phi[3, r], np.linalg.norm(out["phi_sums"][:3]) / ns[r], rtol=1e-4, atol=1e-6)
         np.testing.assert_allclose(psi[3, r], np.linalg.norm(out["phi_sums"][3:]) / ns[r], rtol=1e-4, atol=1e-6)
     _whole_ensemble_invariants(arr, ns, 0.12, g0, g1)
+    # every replica against the oracle: values within the FP32 tolerance but for a few in 10^5
+    # (the ill-conditioned directions where the velocity nearly cancels), phi and psi within a
+    # quarter of one particle's largest share and at 1e-4 in all but 1% of the replicas
+    tally, loose = {}, 0
+    for r in range(len(ns)):
+        a, b = off[r], off[r + 1]
+        ids = ((r << lb) | np.arange(ns[r])).astype(np.int32)
+        out = compare_step(orc, om, ps[r].oracle_dict(), _slice(g0, a, b), _slice(g1, a, b), 3, 0, 32, ids=ids,
+                           local_bits=lb, centroid=cen, tally=tally)
+        for gpu, ref in ((phi[3, r], np.linalg.norm(out["phi_sums"][:3]) / ns[r]),
+                         (psi[3, r], np.linalg.norm(out["phi_sums"][3:]) / ns[r])):
+            assert abs(gpu - ref) < 0.5 / ns[r], (r, gpu, ref)
+            loose += abs(gpu - ref) > 1e-4 * ref
+    assert loose <= 0.01 * len(ns), loose
+    outside = sum(v for k, v in tally.items() if k not in ("n", "worst"))
+    assert tally["n"] > 0.99 * sum(ns)
+    assert outside <= 1e-4 * tally["n"] and tally["worst"] < 100.0, tally
+    assert tally["uv"] == 0 and tally["vel_uv"] == 0, tally
     sim.close()
 
 
