@@ -218,6 +218,24 @@ def test_1m_particle_subset_parity(tg, orc):
     assert outside <= 1e-4 * N and tally["worst"] < 100.0, tally
 
 
+def test_1m_particle_fp64_parity(tg, orc):
+    """The FP64 build on the 1,048,576-particle workload: every particle's step against the
+    oracle's at 1e-12, and the order parameters."""
+    mesh = get_mesh(tg, 7, (20.0, 10.0, 10.0))
+    N, p = params_1m(tg, mesh)
+    om, arr = oracle_mesh(orc, mesh)
+    sim = tg.Simulation(mesh, p, N, seed=2, precision=64)
+    sim.start()
+    sim.step(2)
+    g0 = sim.get_state()
+    sim.step(1)
+    g1 = sim.get_state()
+    out = compare_step(orc, om, p.oracle_dict(), g0, g1, 2, 2, 64, centroid=arr["v3"].mean(0))
+    phi, psi = sim.order_parameter()
+    np.testing.assert_allclose(phi[2, 0], np.linalg.norm(out["phi_sums"][:3]) / N, rtol=1e-10)
+    np.testing.assert_allclose(psi[2, 0], np.linalg.norm(out["phi_sums"][3:]) / N, rtol=1e-10)
+
+
 def test_ensemble_parity(tg, orc, mesh_l4, sys100):
     """Ragged ensemble: each replica matches the oracle run with that replica's parameters."""
     om, cen = sys100
