@@ -199,6 +199,36 @@ def test_ragged_ensemble_4096_replicas_parity(tg, orc):
     sim.close()
 
 
+def test_ragged_ensemble_4096_replicas_fp64(tg, orc):
+    """The FP64 build on the batched ragged ensemble (4,096 replicas, 6.75M particles): every
+    replica's step against the oracle's at 1e-12, and its order parameters."""
+    ens = importlib.import_module("2dtissue_gb300.ensemble")
+    mesh = get_mesh(tg, 4, (4.0, 2.0, 2.0))
+    om, arr = oracle_mesh(orc, mesh)
+    cen = arr["v3"].mean(0)
+    n, eta, v0 = ens.ragged_replicas(seed=0, n_replicas=4096)
+    ns = [int(x) for x in n]
+    ps = [tg.Params(radius=0.05, r_max=0.12, v0=float(v), eta=float(e), dt=0.02) for e, v in zip(eta, v0)]
+    sim = tg.Simulation(mesh, ps, ns, seed=0, precision=64)
+    sim.start()
+    sim.step(2)
+    g0 = sim.get_state()
+    sim.step(1)
+    g1 = sim.get_state()
+    phi, psi = sim.order_parameter()
+    assert sim.status() == 0
+    lb = _local_bits(ns)
+    off = np.concatenate([[0], np.cumsum(ns)])
+    for r in range(len(ns)):
+        a, b = off[r], off[r + 1]
+        ids = ((r << lb) | np.arange(ns[r])).astype(np.int32)
+        out = compare_step(orc, om, ps[r].oracle_dict(), _slice(g0, a, b), _slice(g1, a, b), 2, 0, 64, ids=ids,
+                           local_bits=lb, centroid=cen)
+        np.testing.assert_allclose(phi[2, r], np.linalg.norm(out["phi_sums"][:3]) / ns[r], rtol=1e-9, atol=1e-12)
+        np.testing.assert_allclose(psi[2, r], np.linalg.norm(out["phi_sums"][3:]) / ns[r], rtol=1e-9, atol=1e-12)
+    sim.close()
+
+
 # ---------------------------------------------------------------------------------------------
 # differentiable step: 10,000 particles on the (6,3,3) ellipsoid
 # ---------------------------------------------------------------------------------------------
