@@ -356,6 +356,34 @@ def test_bumpy_sphere_512_replica_ensemble(tg, orc, bumpy):
     sim.close()
 
 
+def test_bumpy_sphere_512_replica_ensemble_fp64(tg, orc, bumpy):
+    """The FP64 build on the batched-adjoint workload's whole 512-replica ensemble (5.2M
+    particles, k up to 20): every replica's step and order parameters against the oracle's at
+    1e-12."""
+    mesh, om, cen, _, _ = bumpy
+    rng = np.random.default_rng(5)
+    ns = [int(x) for x in rng.integers(1000, 20001, size=512)]
+    ps = [tg.Params(v0=float(rng.uniform(0.5, 1.5)), k_rep=float(rng.uniform(5, 20)), tau=float(rng.uniform(0.5, 2)),
+                    eta=float(rng.uniform(0.1, 1.0))) for _ in range(512)]
+    sim = tg.Simulation(mesh, ps, ns, seed=1, precision=64)
+    sim.start()
+    sim.step(2)
+    g0 = sim.get_state()
+    sim.step(1)
+    g1 = sim.get_state()
+    phi, psi = sim.order_parameter()
+    assert sim.status() == 0
+    lb = _local_bits(ns)
+    off = np.concatenate([[0], np.cumsum(ns)])
+    for r in range(len(ns)):
+        a, b = off[r], off[r + 1]
+        ids = ((r << lb) | np.arange(ns[r])).astype(np.int32)
+        out = compare_step(orc, om, ps[r].oracle_dict(), _slice(g0, a, b), _slice(g1, a, b), 2, 1, 64, ids=ids,
+                           local_bits=lb, centroid=cen)
+        np.testing.assert_allclose(phi[2, r], np.linalg.norm(out["phi_sums"][:3]) / ns[r], rtol=1e-9, atol=1e-12)
+        np.testing.assert_allclose(psi[2, r], np.linalg.norm(out["phi_sums"][3:]) / ns[r], rtol=1e-9, atol=1e-12)
+    sim.close()
+
 def test_bumpy_sphere_ensemble_adjoint_matches_dual_oracle(tg, orc, bumpy):
     """FP64 build, 4 steps of the 3-replica ensemble (k up to 20)."""
     mesh, om, cen, ns, ps = bumpy
