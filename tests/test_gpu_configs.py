@@ -36,7 +36,10 @@ def _slice(state, a, b):
     return {k: v[a:b] for k, v in state.items()}
 
 
-def _tangent_r3(om, face, duv):
+def _tangent_r3(om, face, duv, J=None):
+    if J is not None:  # every face's chart map, [F][6]
+        Jf = J[np.asarray(face)]
+        return Jf[:, :3] * duv[:, :1] + Jf[:, 3:] * duv[:, 1:]
     dr = np.zeros((len(face), 3))
     for i, f in enumerate(face):
         J, _, _ = om.face_data(int(f))
@@ -44,7 +47,7 @@ def _tangent_r3(om, face, duv):
     return dr
 
 
-def _chain(orc, om, cen, prm, state, ids, lb, seed, t0, T, tgt, phit, dprm=None, duv=None, dth=None):
+def _chain(orc, om, cen, prm, state, ids, lb, seed, t0, T, tgt, phit, dprm=None, duv=None, dth=None, J=None):
     """Loss of T oracle steps of one replica (its ids carry the replica index for the noise) and,
     with tangents, its directional derivative along (dprm, duv, dth)."""
     n = len(state["theta"])
@@ -52,7 +55,7 @@ def _chain(orc, om, cen, prm, state, ids, lb, seed, t0, T, tgt, phit, dprm=None,
               r3d=state["r3d"].copy(), ids=ids)
     dual = dprm is not None
     if dual:
-        ds = dict(uv=duv.copy(), theta=dth.copy(), r3d=_tangent_r3(om, st["face"], duv))
+        ds = dict(uv=duv.copy(), theta=dth.copy(), r3d=_tangent_r3(om, st["face"], duv, J))
     loss, dloss = 0.0, 0.0
     for t in range(T):
         if dual:
@@ -382,6 +385,49 @@ def test_bumpy_sphere_512_replica_ensemble_fp64(tg, orc, bumpy):
                            local_bits=lb, centroid=cen)
         np.testing.assert_allclose(phi[2, r], np.linalg.norm(out["phi_sums"][:3]) / ns[r], rtol=1e-9, atol=1e-12)
         np.testing.assert_allclose(psi[2, r], np.linalg.norm(out["phi_sums"][3:]) / ns[r], rtol=1e-9, atol=1e-12)
+    sim.close()
+
+def test_bumpy_sphere_512_replica_adjoint_fp64(tg, orc, bumpy):
+    """The FP64 adjoint of 3 steps of the batched-adjoint workload's whole 512-replica ensemble
+    (5.2M particles, k up to 20) against the dual-number oracle chained replica by replica: the
+    directional derivative of the summed loss along a random direction of every replica's
+    parameters and of the initial chart positions and angles (1e-6), and the loss (1e-9)."""
+    mesh, om, cen, _, _ = bumpy
+    rng = np.random.default_rng(5)
+    ns = [int(x) for x in rng.integers(1000, 20001, size=512)]
+    ps = [tg.Params(v0=float(rng.uniform(0.5, 1.5)), k_rep=float(rng.uniform(5, 20)), tau=float(rng.uniform(0.5, 2)),
+                    eta=float(rng.uniform(0.1, 1.0))) for _ in range(512)]
+    sim = tg.Simulation(mesh, ps, ns, seed=1, precision=64)
+    sim.start()
+    sim.step(2)
+    s0 = sim.get_state()
+    t0 = sim.step_count
+    T, R, N = 3, len(ns), sum(ns)
+    off = np.concatenate([[0], np.cumsum(ns)])
+    lb = _local_bits(ns)
+    rng = np.random.default_rng(9)
+    tgt = s0["r3d"] + 0.01 * rng.normal(size=(N, 3))
+    phit = np.full((T, R), 0.3)
+    res = sim.adjoint(T, r3d_target=tgt, w_pos=1.0, phi_target=phit, w_phi=1.0)
+    direction = rng.normal(size=(R, len(tg.GRAD_PARAMS)))
+    duv = 1e-2 * rng.normal(size=(N, 2))
+    dth = rng.normal(size=N)
+    J = np.array([om.face_data(f)[0] for f in range(om.F)])
+    loss, dloss = 0.0, 0.0
+    for r in range(R):
+        a, b = off[r], off[r + 1]
+        prm = ps[r].oracle_dict()
+        dprm = {k: 0.0 for k in prm}
+        for j, name in enumerate(tg.GRAD_PARAMS):
+            dprm[GRAD_TO_ORACLE[name]] = direction[r, j]
+        ids = ((r << lb) | np.arange(ns[r])).astype(np.int32)
+        l, dl = _chain(orc, om, cen, prm, _slice(s0, a, b), ids, lb, 1, t0, T, tgt[a:b], phit[:, r], dprm,
+                       duv[a:b], dth[a:b], J=J)
+        loss += l
+        dloss += dl
+    gpu = (res["d_params"] * direction).sum() + (res["d_uv0"] * duv).sum() + res["d_theta0"] @ dth
+    np.testing.assert_allclose(res["loss"], loss, rtol=1e-9)
+    np.testing.assert_allclose(gpu, dloss, rtol=1e-6)
     sim.close()
 
 def test_bumpy_sphere_ensemble_adjoint_matches_dual_oracle(tg, orc, bumpy):
