@@ -518,6 +518,10 @@ void flush_finalize(tds_sim* s, const StepHooks* hk = nullptr) {
     cudaMemsetAsync(s->phi_pending, 0, sizeof(int), s->stream);
 }
 
+// k_order takes two particles per thread from this many particles on: with one, the GPU holds
+// every particle's load chain at once up to ~0.3M particles; with two, a system needs ~0.6M to fill it
+constexpr int kOrderPairN = 1 << 19;
+
 // Buffer roles: index 0 = step output (and set_state target), index 1 = sorted copy.
 template <typename real>
 void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullptr, int* nbr_list = nullptr,
@@ -545,9 +549,16 @@ void launch_one_step(tds_sim* s, const real* noise, const StepHooks* hk = nullpt
     }
     {
         KernelTimer kt(s, 2);
-        tdsk::k_order<real><<<nb, 256, 0, st>>>(s->tmp, s->key[o], s->ids[o], start, (const R4<real>*)s->pos[o],
-                                                 (const R4<real>*)s->pol[o], (const R2<real>*)s->uv[o], cpos, cpol,
-                                                 cuv, cids, ckey, s->N);
+        // two particles per thread on a large system (their load chains in flight together: the
+        // 4,096-replica ensemble's k_order 121 -> 110 us); one on a small one, which needs the blocks
+        if (s->N >= kOrderPairN)
+            tdsk::k_order<real, 2><<<(s->N + 511) / 512, 256, 0, st>>>(
+                s->tmp, s->key[o], s->ids[o], start, (const R4<real>*)s->pos[o], (const R4<real>*)s->pol[o],
+                (const R2<real>*)s->uv[o], cpos, cpol, cuv, cids, ckey, s->N);
+        else
+            tdsk::k_order<real, 1><<<nb, 256, 0, st>>>(s->tmp, s->key[o], s->ids[o], start,
+                                                        (const R4<real>*)s->pos[o], (const R4<real>*)s->pol[o],
+                                                        (const R2<real>*)s->uv[o], cpos, cpol, cuv, cids, ckey, s->N);
     }
     tdsk::StepArgs<real> a;
     a.pos = cpos;

@@ -1010,26 +1010,50 @@ __global__ void k_scatter(const int* __restrict__ key, int* __restrict__ count, 
 
 // Within each cell, particles in increasing particle-id order: the particle in slot s goes to
 // start[b] + (number of the cell's particles with a smaller id); its state is copied there.
-template <typename real>
-__global__ void k_order(const int* __restrict__ tmp, const int* __restrict__ key, const int* __restrict__ ids,
-                        const int* __restrict__ start, const R4<real>* __restrict__ pos,
-                        const R4<real>* __restrict__ pol, const R2<real>* __restrict__ uv, R4<real>* __restrict__ spos,
-                        R4<real>* __restrict__ spol, R2<real>* __restrict__ suv, int* __restrict__ sids,
-                        int* __restrict__ skey, int N) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= N) return;
-    const int s = tmp[p];
-    const int b = key[s];
-    const int me = ids[s];
-    const int b0 = start[b], b1 = start[b + 1];
-    int rank = 0;
-    for (int x = b0; x < b1; ++x) rank += ids[tmp[x]] < me;
-    const int d = b0 + rank;
-    spos[d] = pos[s];
-    spol[d] = pol[s];
-    suv[d] = uv[s];
-    sids[d] = me;
-    skey[d] = b;
+// PPT particles per thread (p, p + 256, ... of a block's 256 * PPT): the chains of dependent
+// loads of the thread's particles (slot -> cell and id -> cell starts -> the cell's other ids)
+// are interleaved, so that more of them are in flight at once.
+template <typename real, int PPT>
+__global__ void __launch_bounds__(256) k_order(const int* __restrict__ tmp, const int* __restrict__ key,
+                                               const int* __restrict__ ids, const int* __restrict__ start,
+                                               const R4<real>* __restrict__ pos, const R4<real>* __restrict__ pol,
+                                               const R2<real>* __restrict__ uv, R4<real>* __restrict__ spos,
+                                               R4<real>* __restrict__ spol, R2<real>* __restrict__ suv,
+                                               int* __restrict__ sids, int* __restrict__ skey, int N) {
+    int s[PPT], b[PPT], me[PPT], c0[PPT], c1[PPT], rank[PPT];
+#pragma unroll
+    for (int i = 0; i < PPT; ++i) {
+        const int p = (int)blockIdx.x * 256 * PPT + i * 256 + (int)threadIdx.x;
+        s[i] = p < N ? tmp[p] : -1;
+    }
+#pragma unroll
+    for (int i = 0; i < PPT; ++i) {
+        b[i] = s[i] >= 0 ? key[s[i]] : 0;
+        me[i] = s[i] >= 0 ? ids[s[i]] : 0;
+    }
+    int len = 0;
+#pragma unroll
+    for (int i = 0; i < PPT; ++i) {
+        c0[i] = s[i] >= 0 ? start[b[i]] : 0;
+        c1[i] = s[i] >= 0 ? start[b[i] + 1] : 0;
+        rank[i] = 0;
+        len = max(len, c1[i] - c0[i]);
+    }
+    for (int k = 0; k < len; ++k) {
+#pragma unroll
+        for (int i = 0; i < PPT; ++i)
+            if (c0[i] + k < c1[i]) rank[i] += ids[tmp[c0[i] + k]] < me[i];
+    }
+#pragma unroll
+    for (int i = 0; i < PPT; ++i) {
+        if (s[i] < 0) continue;
+        const int d = c0[i] + rank[i];
+        spos[d] = pos[s[i]];
+        spol[d] = pol[s[i]];
+        suv[d] = uv[s[i]];
+        sids[d] = me[i];
+        skey[d] = b[i];
+    }
 }
 
 // Per-tile sums of the cell counts (one block per scan tile), written into the tile counts of the
