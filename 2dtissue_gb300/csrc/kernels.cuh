@@ -995,17 +995,28 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(int* __restrict__ count, 
 }
 
 // Counting-sort scatter; the cell's count is the cursor and ends at zero for the next step.
-__global__ void k_scatter(const int* __restrict__ key, int* __restrict__ count, const int* __restrict__ start,
-                          int* __restrict__ tmp, int N, long long* d_step, int* phi_pending) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s == 0) {
+// PPT slots per thread (s, s + 256, ... of a block's 256 * PPT), their returning atomics in flight
+// together.
+template <int PPT>
+__global__ void __launch_bounds__(256) k_scatter(const int* __restrict__ key, int* __restrict__ count,
+                                                 const int* __restrict__ start, int* __restrict__ tmp, int N,
+                                                 long long* d_step, int* phi_pending) {
+    const int s0 = (int)blockIdx.x * 256 * PPT + (int)threadIdx.x;
+    if (s0 == 0) {
         *d_step += 1;
         *phi_pending = 0;  // k_scan has finalized the previous step
     }
-    if (s < N) {
-        const int b = key[s];
-        tmp[start[b] + atomicSub(&count[b], 1) - 1] = s;
+    int b[PPT], c[PPT], r[PPT];
+#pragma unroll
+    for (int i = 0; i < PPT; ++i) b[i] = s0 + i * 256 < N ? key[s0 + i * 256] : -1;
+#pragma unroll
+    for (int i = 0; i < PPT; ++i) {
+        c[i] = b[i] >= 0 ? start[b[i]] : 0;
+        r[i] = b[i] >= 0 ? atomicSub(&count[b[i]], 1) : 0;
     }
+#pragma unroll
+    for (int i = 0; i < PPT; ++i)
+        if (b[i] >= 0) tmp[c[i] + r[i] - 1] = s0 + i * 256;
 }
 
 // Within each cell, particles in increasing particle-id order: the particle in slot s goes to
